@@ -1,0 +1,404 @@
+"""Generate the golden fixtures under ``tests/golden/`` from the reference.
+
+This script is test infrastructure.  It imports the unmodified reference
+package (monashNV/superspinsim 1.3.2) from ``$SSS_REFERENCE`` (default
+``/root/reference``) and runs its own CPU path.  numba and qutip are not
+installed here, so a small import shim stands in for them:
+
+* ``numba.jit`` becomes the identity and ``numba.prange`` becomes ``range``
+  (the reference's CPU kernels then run as plain Python loops, with Python's
+  float64 arithmetic and no fast-math reassociation);
+* ``numba.cuda`` is a sequential stand-in that runs each of the
+  reference's GPU kernels once per thread index in Python (``nc.fma`` is
+  an unfused multiply-add).  Runs use the reference's GPU branch by
+  default -- the branch that produced its golden CSVs -- because its CPU
+  rotating-frame branch indexes out of bounds
+  (``superspinsim/generate_simulator.py:985``, loop bound ``doubles_size``
+  instead of ``singles_size``); cases marked ``path="cpu"`` take the CPU
+  branch (``use_cuda=False``) to pin it too;
+* ``qutip.Qobj`` is an empty class (only used in ``isinstance`` checks,
+  ``superspinsim/sugar.py:181``).
+
+For each case the fixture stores the reference's generators
+(``generate_atoms``, ``superspinsim/generate_generators.py:19-166``), its
+vectorisation map, the generalised-rotating-frame arrays when used
+(``make_rotating``, ``:2491-2519``), the coefficient program in this
+project's segment format, and the density operators returned by
+``simulate`` (``superspinsim/generate_simulator.py:1508-2200``) on a short
+window.  Where the case is one of the reference's golden regression tests,
+the leading values of its CSV (``test/reference/*.csv``) are stored too.
+
+Run:  python tests/golden/make_golden.py            (about 5 minutes, 1 core)
+"""
+import math
+import os
+import sys
+import tempfile
+import time as _time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE = os.environ.get("SSS_REFERENCE", "/root/reference")
+
+_SHIM = {
+    "numba/__init__.py": (
+        "def jit(*args, **kwargs):\n"
+        "    if len(args) == 1 and callable(args[0]):\n"
+        "        return args[0]\n"
+        "    return lambda f: f\n"
+        "prange = range\n"
+        "from . import core\n"),
+    "numba/core/__init__.py": "from . import errors\n",
+    "numba/core/errors.py":
+        "class NumbaPerformanceWarning(Warning):\n    pass\n",
+    "qutip/__init__.py": "class Qobj:\n    pass\n",
+    # Sequential stand-in for numba.cuda: each kernel launch runs its
+    # Python body once per (block, thread) index, in order.  The
+    # reference's kernels use no shared memory or barriers (the only uses
+    # are in commented-out code), and none of them writes an array that
+    # another thread of the same launch reads, so sequential execution
+    # gives the same result as a GPU.  nc.fma is an unfused a*b + c.
+    "numba/cuda/__init__.py": (
+        "import numpy as _np\n"
+        "class _Dim:\n"
+        "    def __init__(self):\n"
+        "        self.x = self.y = self.z = 0\n"
+        "threadIdx, blockIdx, blockDim = _Dim(), _Dim(), _Dim()\n"
+        "def fma(a, b, c):\n"
+        "    return a*b + c\n"
+        "class DeviceArray(_np.ndarray):\n"
+        "    def copy_to_host(self):\n"
+        "        return _np.array(self)\n"
+        "def device_array(shape, dtype=_np.float64):\n"
+        "    return _np.zeros(shape, dtype).view(DeviceArray)\n"
+        "def to_device(a):\n"
+        "    return _np.array(a).view(DeviceArray)\n"
+        "def _dims(d):\n"
+        "    d = tuple(d) if isinstance(d, (tuple, list)) else (d,)\n"
+        "    return tuple(int(v) for v in d) + (1,)*(3 - len(d))\n"
+        "class _Kernel:\n"
+        "    def __init__(self, f):\n"
+        "        self.f = f\n"
+        "    def __getitem__(self, cfg):\n"
+        "        grid, block = _dims(cfg[0]), _dims(cfg[1])\n"
+        "        def launch(*args):\n"
+        "            blockDim.x, blockDim.y, blockDim.z = block\n"
+        "            for bz in range(grid[2]):\n"
+        "                for by in range(grid[1]):\n"
+        "                    for bx in range(grid[0]):\n"
+        "                        blockIdx.x, blockIdx.y, blockIdx.z = bx, by, bz\n"
+        "                        for tz in range(block[2]):\n"
+        "                            for ty in range(block[1]):\n"
+        "                                for tx in range(block[0]):\n"
+        "                                    threadIdx.x = tx\n"
+        "                                    threadIdx.y = ty\n"
+        "                                    threadIdx.z = tz\n"
+        "                                    self.f(*args)\n"
+        "        return launch\n"
+        "def jit(f=None, device=False, **kwargs):\n"
+        "    if f is None:\n"
+        "        return lambda g: jit(g, device=device)\n"
+        "    return f if device else _Kernel(f)\n"),
+}
+
+
+def install_shim():
+    root = tempfile.mkdtemp(prefix="sss_shim_")
+    for rel, text in _SHIM.items():
+        path = os.path.join(root, rel)
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            f.write(text)
+    sys.path.insert(0, REFERENCE)
+    sys.path.insert(0, root)
+
+
+# Coefficient programs ------------------------------------------------------
+# A program is, per control channel (x, y, z field in tesla; r = optical
+# excitation), a list of segments (t_end, offset, amplitude, frequency,
+# phase): for t < t_end (first match) the channel is
+# offset + amplitude*cos(tau*frequency*t + phase); after the last segment
+# it is 0.
+
+
+def channel_fn(segs):
+    segs = [tuple(float(v) for v in s) for s in segs]
+
+    def fn(t):
+        for t_end, off, amp, freq, ph in segs:
+            if t < t_end:
+                return off + amp*math.cos(math.tau*freq*t + ph)
+        return 0.0
+    return fn
+
+
+def drive(freq, amp, t_end=1.0, phase=0.0, offset=0.0):
+    return [(t_end, offset, amp, freq, phase)]
+
+
+def const(value, t_end=1.0):
+    return [(t_end, value, 0.0, 0.0, 0.0)]
+
+
+def program_array(channels):
+    """Pack the 4 channels as a (4, S, 5) float64 array (S = max segments,
+    missing segments padded with t_end = -inf so they never match)."""
+    smax = max(1, max(len(c) for c in channels))
+    out = np.zeros((4, smax, 5))
+    out[:, :, 0] = -np.inf
+    for g, segs in enumerate(channels):
+        for s, seg in enumerate(segs):
+            out[g, s, :] = seg
+    return out
+
+
+# Cases --------------------------------------------------------------------
+B0 = np.array([0, 0, 1e-3])
+QUBIT = [[{"S": 1/2, "g": 2.0, "B0": B0}]]
+QUTRIT = [[{"S": 1, "g": -1/2, "D": 72, "B0": B0}]]
+
+
+def qubit_t1(temp):
+    return [[{"S": 1/2, "g": 2.0, "B0": B0, "TS1": 1e-6, "T": temp}]]
+
+
+QUBIT_HF = [[{"S": 1/2, "g": 2.0, "B0": B0, "I": 1/2, "g": 1.0, "A": 2e9}]]
+QUTRIT_HF = [[{"S": 1, "g": -1/2, "D": 72, "B0": B0, "I": 1/2, "gI": 1.0,
+               "A": 2e9}]]
+
+
+def spin1_c1():
+    """Spin-1 NV ground state, 10 mT along z, Lindblad dephasing and T1."""
+    return [[{"S": 1, "g": 28.025e9/13996244917.1, "D": math.tau*2.870e9,
+              "B0": np.array([0, 0, 0.01]), "TS2": 1e-6, "TS1": 1e-3,
+              "T": 293.15}]]
+
+
+T1_END = 1/(2*10e-3*28e9)
+ZERO = const(0.0)
+
+
+def cases():
+    q_drive = drive(28e6, 10e-6)
+    t_drive = drive(7e6, 10e-6)
+    c1_drive = drive(2.870e9 + 28.025e9*0.01 + 5e6, 10e6/28.025e9)
+    rho_q0 = np.diag([1.0, 0.0]).astype(complex)
+    rho_q1 = np.diag([0.0, 1.0]).astype(complex)
+    rho_t2 = np.diag([0.0, 0.0, 1.0]).astype(complex)
+    rho_tu = np.eye(3, dtype=complex)/3
+    rho_hf = np.zeros((4, 4), complex)
+    rho_hf[0, 0] = 1
+    rho_c1 = np.diag([0.0, 1.0, 0.0]).astype(complex)
+    base = dict(spin_interactions=[{}], group_interactions={},
+                use_kernel=False, use_unitary=False, use_incoherent=True,
+                R=35)
+    out = [
+        dict(name="qubit_couple", csv="qubit-couple", spins=QUBIT,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0, t=(0, 20e-9, 1e-9),
+             rot=False, res=False, K=1, F=100),
+        dict(name="qubit_couple_res_e2", csv="qubit-couple", spins=QUBIT,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0, t=(0, 20e-9, 1e-9),
+             rot=False, res=True, K=2, F=10),
+        dict(name="qubit_couple_res_e2_cpu", csv="qubit-couple",
+             spins=QUBIT, ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0,
+             t=(0, 20e-9, 1e-9), rot=False, res=True, K=2, F=10,
+             path="cpu"),
+        dict(name="qubit_couple_res_e5", csv="qubit-couple", spins=QUBIT,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0, t=(0, 10e-9, 1e-9),
+             rot=False, res=True, K=5, F=10),
+        dict(name="qubit_couple_res_e3_e6", csv="qubit-couple", spins=QUBIT,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0, t=(0, 6e-9, 1e-9),
+             rot=False, res=True, K=3, F=10, K2=6),
+        dict(name="qubit_t1_0K", csv="qubit-t1-0K", spins=qubit_t1(0),
+             ch=[drive(28e6, 10e-3, t_end=T1_END), ZERO, ZERO, ZERO],
+             rho0=rho_q1, t=(0, 20e-9, 1e-9), rot=False, res=True, K=1,
+             F=100),
+        dict(name="qubit_t1_mK", csv="qubit-t1-mK", spins=qubit_t1(1e-3),
+             ch=[drive(28e6, 10e-3, t_end=T1_END), ZERO, ZERO, ZERO],
+             rho0=rho_q1, t=(0, 20e-9, 1e-9), rot=False, res=True, K=1,
+             F=100),
+        dict(name="qutrit_couple", csv="qutrit-couple", spins=QUTRIT,
+             ch=[t_drive, ZERO, ZERO, ZERO], rho0=rho_t2, t=(0, 5e-9, 1e-9),
+             rot=False, res=True, K=1, F=100),
+        dict(name="qutrit_couple_unital", csv="qutrit-couple-unital",
+             spins=QUTRIT, ch=[t_drive, ZERO, ZERO, ZERO], rho0=rho_tu,
+             t=(0, 5e-9, 1e-9), rot=False, res=True, K=1, F=100),
+        dict(name="qubit_hyperfine", csv="qubit-hyperfine", spins=QUBIT_HF,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_hf, t=(0, 1e-9, 1e-9),
+             rot=True, res=True, K=1, F=100),
+        dict(name="qubit_couple_rot_e5", csv="qubit-couple", spins=QUBIT,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0, t=(0, 10e-9, 1e-9),
+             rot=True, res=True, K=5, F=10),
+        dict(name="qubit_couple_rot_e1_nores", csv="qubit-couple",
+             spins=QUBIT, ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0,
+             t=(0, 10e-9, 1e-9), rot=True, res=False, K=1, F=10),
+        dict(name="spin1_c1", csv=None, spins=spin1_c1(),
+             ch=[c1_drive, ZERO, ZERO, ZERO], rho0=rho_c1,
+             t=(0, 1e-9, 1e-9), rot=False, res=True, K=2, F=100,
+             use_incoherent=False),
+        dict(name="qutrit_hyperfine", csv="qutrit-hyperfine",
+             spins=QUTRIT_HF, ch=[t_drive, ZERO, ZERO, ZERO],
+             rho0=np.diag([1.0, 0, 0, 0, 0, 0]).astype(complex),
+             t=None, rot=True, res=True, K=1, F=100),
+    ]
+    for c in out:
+        for k, v in base.items():
+            c.setdefault(k, v)
+    return out
+
+
+def nv7_case(name, use_incoherent, t, F, K=2, extra=None):
+    """The 7-level NV model (reference ``models.nv_7``) at B = 5 mT along z
+    with the rates of the 7-level ODMR workload, driven by an x field
+    at the ms=0 -> +1 resonance plus 5 MHz detuning, laser at 10/65.9 of
+    saturation (pump rate 10 /us)."""
+    from superspinsim import models, params
+    P = nv7_params(params)
+    spins, inter, groups = models.nv_7(np.array([0, 0, 5e-3]), params=P)
+    f_res = 2.870e9 + 28.025e9*5e-3
+    amp = 5e6/28.025e9
+    rho0 = np.zeros((7, 7), complex)
+    rho0[1, 1] = 1.0
+    c = dict(name=name, csv=None, spins=spins, spin_interactions=inter,
+             group_interactions=groups,
+             ch=[drive(f_res + 5e6, amp), ZERO, ZERO, const(10/65.9)],
+             rho0=rho0, t=t, rot=False, res=True, K=K, F=F,
+             use_incoherent=use_incoherent, use_kernel=False,
+             use_unitary=False, R=35)
+    if extra:
+        c.update(extra)
+    return c
+
+
+def nv7_params(params):
+    """The reference's parameter module with the 7-level ODMR workload's
+    rates: ground D = 2.870 GHz, excited D = 1.42 GHz, spin-conserving
+    optical decay 65.9 /us, ISC 11 /us (ms=0) and 80 /us (ms=+-1) into the
+    singlet, singlet decay 3.0 /us to ms=0 and 2.6 /us to ms=+-1."""
+    import copy
+    import types
+    P = types.SimpleNamespace()
+    P.fundamental = params.fundamental
+    P.standards = params.standards
+
+    class ground(params.nv.room.ground):
+        zfs_longitudinal = 2.870e9
+
+    class excited(params.nv.room.excited):
+        zfs_longitudinal = 1.42e9
+
+    class optical(params.nv.room.optical):
+        conserving = 65.9e6
+        nonconserving = None
+
+    class isc(params.nv.room.isc):
+        s_gets_z = 11e6
+        s_gets_pm = 80e6
+        z_gets_s = 3.0e6
+        pm_gets_s = 2.6e6
+
+    class room:
+        pass
+    room.ground, room.excited, room.optical, room.isc = \
+        ground, excited, optical, isc
+
+    class nv:
+        pass
+    nv.room = room
+    P.nv = nv
+    return copy.copy(P)
+
+
+def build_generators(c):
+    from superspinsim.generate_generators import generate_atoms, \
+        make_rotating
+    g, vmap = generate_atoms(
+        c["spins"], c["spin_interactions"], c["group_interactions"],
+        False, True, c["use_incoherent"])
+    gens = [g["generators"][k] for k in ["L0", "Gx", "Gy", "Gz", "Gr"]]
+    out = dict(generators=np.array(gens), vectorisation_map=vmap)
+    if c["rot"]:
+        gr, V, Vi, D, S = make_rotating(gens[0], gens[1:])
+        out.update(generators_rotating=np.array(gr), vectors_real=V,
+                   inv_vectors_real=Vi, doubles=D.reshape(-1, 2),
+                   singles=S)
+    return out
+
+
+def run_reference(c, K=None):
+    from superspinsim import simspins
+    fns = [channel_fn(s) for s in c["ch"]]
+    t0, tf, dt = c["t"]
+    _, dens = simspins(
+        fns, t0, tf, dt, c["spins"], c["spin_interactions"],
+        c["group_interactions"], c["rho0"],
+        number_of_exponentials=K or c["K"],
+        number_of_fine_divisions=c["F"],
+        number_of_quadratic_repeats=c["R"], use_rotating=c["rot"],
+        use_residual=c["res"], use_kernel=False, use_unitary=False,
+        use_cuda=(c.get("path", "gpu") == "gpu"), use_hermitian=True,
+        use_incoherent=c["use_incoherent"])
+    return dens
+
+
+def csv_prefix(name, count=400):
+    path = os.path.join(REFERENCE, "test", "reference", name + ".csv")
+    return np.loadtxt(path, delimiter=",")[:count]
+
+
+def save_case(c, extra_runs=()):
+    t_start = _time.time()
+    arrays = build_generators(c)
+    arrays["program"] = program_array(c["ch"])
+    arrays["rho0"] = c["rho0"]
+    meta = dict(rot=c["rot"], res=c["res"], K=c["K"], F=c["F"], R=c["R"],
+                use_incoherent=c["use_incoherent"],
+                path=c.get("path", "gpu"))
+    if c["t"] is not None:
+        arrays["times"] = np.array(c["t"], dtype=float)
+        arrays["density"] = run_reference(c)
+        for K2 in extra_runs:
+            arrays[f"density_K{K2}"] = run_reference(c, K=K2)
+    if c["csv"]:
+        arrays["csv_prefix"] = csv_prefix(c["csv"])
+    for k, v in meta.items():
+        arrays["meta_" + k] = np.array(v)
+    path = os.path.join(HERE, c["name"] + ".npz")
+    np.savez_compressed(path, **arrays)
+    print(f"{c['name']}: N={arrays['generators'].shape[1]} "
+          f"{_time.time() - t_start:.1f} s", flush=True)
+
+
+def save_quadratures():
+    """The reference's Gauss-Legendre nodes and commutator-free weights
+    (``superspinsim/quadratures.py:10-50``)."""
+    from superspinsim.quadratures import samples, weights
+    arrays = {}
+    for k, v in samples.items():
+        arrays["samples_" + k] = np.asarray(v, dtype=np.float64)
+    for k, v in weights.items():
+        arrays["weights_" + k] = np.asarray(v, dtype=np.float64)
+    np.savez(os.path.join(HERE, "quadratures.npz"), **arrays)
+
+
+def main():
+    install_shim()
+    only = set(sys.argv[1:])
+    save_quadratures()
+    for c in cases():
+        if only and c["name"] not in only:
+            continue
+        save_case(c, extra_runs=(c["K2"],) if "K2" in c else ())
+    extra = [
+        nv7_case("nv7_n49", False, (0, 10e-12, 10e-12), F=2),
+        nv7_case("nv7_n19", True, (0, 20e-12, 10e-12), F=2),
+    ]
+    for c in extra:
+        if only and c["name"] not in only:
+            continue
+        save_case(c)
+
+
+if __name__ == "__main__":
+    main()
