@@ -1,0 +1,347 @@
+"""Throughput benchmark: the 7-level NV ODMR sweep.
+
+Workload (one bench step): 1024 microwave frequencies uniform over
++-30 MHz around the ms=0 -> +1 resonance of the 7-level NV model (ground
+D = 2.870 GHz, excited D = 1.42 GHz, B = 5 mT along z, optical decay
+65.9 /us, ISC 11 /us and 80 /us, singlet decay 3.0 /us and 2.6 /us), Rabi
+5 MHz, laser pumping 10 /us; each trajectory 2 us at dt = 5 ps with the
+4th-order commutator-free Magnus method (CF4:2), 400,000 steps, readout
+of the excited-state population every 1 ns (T = 2000, F = 200), vectorised
+density of length 49 (Liouvillian 49 x 49, float64).  Unit: trajectory
+steps per second, one trajectory step = one CF4:2 step of one trajectory.
+
+Arms:
+  default           the batched persistent kernel of libsss.so.  `value`
+                    times sss_batch_run on device-resident inputs; `e2e`
+                    times the public API (superspinsim_gb300.sweep.Sweep.run)
+                    from host buffers to host readouts.
+  --impl reference  the reference's algorithm on the host cores: the CPU
+                    oracle (a C/OpenMP restatement of the reference's
+                    simulate -- 2R = 70 dense squarings per exponential,
+                    serial chain of step propagators) on a bounded sample
+                    of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_FREQ = 1024
+DURATION = 2e-6
+DT_OUT = 1e-9
+F = 200
+K_EXP = 2
+B_FIELD = 5e-3
+GAMMA = 28.025e9
+F_RES = 2.870e9 + GAMMA*B_FIELD
+RABI = 5e6
+LASER = 10/65.9
+METRIC = "NV-7 ODMR traj-steps/s"
+
+
+def nv7_model():
+    """Generators (5, 49, 49) and vectorisation map of the 7-level NV at
+    B = 5 mT with the workload's rates."""
+    from superspinsim_gb300 import models
+    from superspinsim_gb300.generators import generate_atoms
+    spins, inter, groups = models.nv_7(np.array([0.0, 0.0, B_FIELD]),
+                                       params=models.odmr_params())
+    g, vm = generate_atoms(spins, inter, groups, use_incoherent=False)
+    gens = np.array([g["generators"][k] for k in ("L0", "Gx", "Gy", "Gz", "Gr")])
+    return gens, vm
+
+
+def workload(n_freq=N_FREQ):
+    freqs = F_RES + np.linspace(-30e6, 30e6, n_freq)
+    progs = np.zeros((n_freq, 4, 1, 5))
+    progs[:, :, :, 0] = np.inf
+    progs[:, 0, 0, 2] = RABI/GAMMA
+    progs[:, 0, 0, 3] = freqs
+    progs[:, 3, 0, 1] = LASER
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1.0
+    return progs, rho
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples taken while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0] or None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        _ = dev
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def flops_per_traj_step(info, G, K):
+    """Executed FP64 flops of one trajectory step of the batched kernel:
+    per exponential and sub-step, assembly of Omega on the pruned pattern
+    (2 G nnz) and d Taylor terms (2 nnz multiply-adds + 2 rows for the
+    scaling and accumulation)."""
+    nnz, rows, d, m = info["nnz"], info["rows"], info["degree"], info["substeps"]
+    return K*(2*G*nnz + m*d*(2*nnz + 2*rows))
+
+
+def cpu_baseline(steps=None, threads=0):
+    """The reference's algorithm (CPU oracle, reference mode) on a bounded
+    sample of the workload: one trajectory, 64 output samples of F = 50
+    fine steps at the workload's 5 ps step (3200 trajectory steps), on all
+    host cores (OpenMP over output samples)."""
+    from oracle import oracle
+    from superspinsim_gb300.quadratures import method
+    gens, vm = nv7_model()
+    progs, rho = workload(1)
+    W, nodes = method(K_EXP)
+    T_s, F_s = 64, 50
+    dt_s = F_s*(DT_OUT/F)
+    t = time.perf_counter()
+    oracle.simulate(gens, rho, 0.0, T_s*dt_s + dt_s*1e-4, dt_s, progs[0], K=K_EXP, W=W,
+                    nodes=nodes, F=F_s, R=35, residual=True, vectorisation_map=vm,
+                    mode="reference", threads=threads)
+    el = time.perf_counter() - t
+    n = T_s*F_s
+    return {"value": n/el, "unit": "traj-steps/s",
+            "cores": threads or oracle.max_threads(), "kind": "port",
+            "sample": f"1 trajectory x {n} CF4:2 steps (64 samples x F=50) of the "
+                      f"workload, reference algorithm (70 squarings per exponential)",
+            "seconds": el}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    samples = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline()
+        if i >= args.warmup:
+            samples.append(r)
+    total_steps = sum(r["value"]*r["seconds"] for r in samples)
+    total_time = sum(r["seconds"] for r in samples)
+    v = total_steps/total_time
+    cb = dict(samples[0])
+    cb["value"] = v
+    cb.pop("seconds", None)
+    line = {"metric": METRIC, "value": v, "unit": "traj-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3*total_time/args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "NV-7 ODMR sweep (bounded CPU sample)", "n_levels": 7,
+                       "liouvillian": "49x49", "method": "CF4:2", "dt_s": DT_OUT/F,
+                       "parallelism": "host cores"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "traj-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-freq", type=int, default=N_FREQ)
+    ap.add_argument("--duration", type=float, default=DURATION)
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+
+    import torch
+    from superspinsim_gb300 import _lib
+    from superspinsim_gb300.generate_simulator import flatten_density
+    from superspinsim_gb300.sweep import Sweep, population_weights, trapezoid
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    gens, vm = nv7_model()
+    N = vm.shape[0]
+    progs, rho = workload(args.n_freq)
+    B = progs.shape[0]
+    T = int(round(args.duration/DT_OUT))
+    rho0 = np.repeat(flatten_density(rho, N, vm)[None], B, axis=0)
+    w = population_weights(vm, [3, 4, 5])
+    sweep = Sweep(gens, vm, number_of_exponentials=K_EXP, number_of_fine_divisions=F,
+                  lanes=args.lanes)
+    plan = sweep.plan
+
+    stream = torch.cuda.Stream()
+    d_rho0 = torch.from_numpy(rho0).cuda()
+    d_prog = torch.from_numpy(progs).cuda()
+    d_ro = torch.empty((B, T), dtype=torch.float64, device="cuda")
+    flush = torch.empty(256*1024*1024//4, dtype=torch.float32, device="cuda")  # > L2
+
+    def step():
+        plan.batch_device(d_rho0.data_ptr(), B, d_prog.data_ptr(), 4, progs.shape[2], 0.0,
+                          DT_OUT, T, F, readout_weights=w, readout_ptr=d_ro.data_ptr(),
+                          stream=stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        clocks = ClockSampler()
+        clocks.start()
+        times, kernel_ms = [], []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            barrier(world)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+            kernel_ms.append(plan.batch_info()["kernel_ms"])
+        barrier(world)
+        clock_info = clocks.stop()
+    info = plan.batch_info()
+    launches = plan.last_launches()*args.steps
+    total_ms = max_over_ranks(sum(times), world)
+    units = B*T*F*world*args.steps
+    value = units/(total_ms/1e3)
+
+    # e2e: public API, host buffers in and out, every step
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        barrier(world)
+        t = time.perf_counter()
+        out = sweep.run(np.repeat(rho[None], B, axis=0), progs, 0.0, args.duration + 1e-13,
+                        DT_OUT, readout_weights=w)
+        fluor = 65.9e6*trapezoid(out["readout"], DT_OUT)
+        el = time.perf_counter() - t
+        if i >= args.warmup:
+            e2e_times.append(el)
+    e2e_s = max_over_ranks(sum(e2e_times), world)
+    e2e_value = B*T*F*world*args.steps/e2e_s
+    h2d = rho0.nbytes + progs.nbytes
+    d2h = B*T*8
+
+    fl = flops_per_traj_step(info, gens.shape[0], K_EXP)
+    kms = statistics.mean(kernel_ms)
+    achieved = fl*B*T*F/(kms*1e-3)/1e12
+    peak = _lib.fp64_peak_tflops()
+    line = {"metric": METRIC, "value": value, "unit": "traj-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms/args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "NV-7 ODMR sweep, 1024 frequencies x 2 us at 5 ps "
+                                   "(400k CF4:2 steps each), readout every 1 ns",
+                       "n_freq": B, "n_levels": 7, "liouvillian": "49x49", "method": "CF4:2",
+                       "dt_s": DT_OUT/F, "samples": T, "fine_divisions": F,
+                       "traj_steps_per_step": B*T*F,
+                       "l2": "flushed between timed steps (256 MiB write)",
+                       "kernel": {"lanes": info["lanes"], "taylor_degree": info["degree"],
+                                  "substeps": info["substeps"], "rows": info["rows"],
+                                  "nnz": info["nnz"]},
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "traj-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved/peak, "traffic": None,
+                         "peak_source": "measured live (sss_fp64_peak DFMA loop)",
+                         "flops_per_traj_step": fl},
+            "clocks": clock_info,
+            "fluorescence_check": float(np.mean(fluor))}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline()
+        cb.pop("seconds", None)
+        line["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/*
+ * sss.h -- C-ABI of libsss.so, the GB300 (sm_103a) time-stepping core of
+ * superspinsim_gb300.
+ *
+ * The reference (monashNV/superspinsim 1.3.2) is pure Python: its hot path
+ * is the closure built by `generate_simulator(...)`
+ * (superspinsim/generate_simulator.py:17-154) and the `simulate(rho0, t0,
+ * tf, dt)` function it returns (:1508-2200), whose device work is a set of
+ * numba.cuda kernels launched from Python.  A Python caller of this library
+ * (superspinsim_gb300/generate_simulator.py, through ctypes) keeps that
+ * API; these entry points replace the numba kernels and their host driver
+ * loop:
+ *
+ *   sss_plan_create    replaces generate_simulator's set-up
+ *                      (:49-154: flag handling, 4^R scaling, CF table
+ *                      selection, generator cast and upload :1697-1811)
+ *   sss_plan_set_rotating  the generalised-rotating-frame set-up
+ *                      (:142-151, host frame preparation :1567-1677)
+ *   sss_simulate       `simulate` (:1508-2200) for one or more trajectories:
+ *                      the fine-step loop :1954-2015, the chain :2025-2028,
+ *                      the frame sandwich :2030-2038 and rho(t) = U(t) rho0
+ *                      :2111-2116.  Host buffers in and out.
+ *   sss_simulate_device  the same on device pointers (inputs resident in
+ *                      HBM), for callers that own device memory.
+ *   sss_batch_run      no single reference counterpart: the batched sweep
+ *                      that replaces calling `simspins` in a loop
+ *                      (superspinsim/sugar.py:566-583) once per parameter
+ *                      point.  Persistent kernel, device work queue.
+ *   sss_last_error / sss_plan_destroy   error text and teardown.
+ *
+ * Conventions.  All arithmetic is IEEE binary64.  Matrices are row-major.
+ * A state is the real vectorised density operator of length N in the
+ * reference's Hermitian basis (vectorisation_map rows (y, x, c),
+ * superspinsim/generate_generators.py:2361-2382).  Every entry point
+ * returns 0 on success or a negative SSS_E* code; nothing aborts or throws
+ * across the ABI, and sss_last_error() gives a thread-local message.
+ * A plan owns its device memory; host buffers stay caller-owned and are
+ * only touched during the call.  A plan is not thread-safe: use one plan
+ * per host thread.
+ */
+#ifndef SSS_H
+#define SSS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SSS_OK 0
+#define SSS_EINVAL (-1)     /* bad shape or argument */
+#define SSS_ENOMEM (-2)     /* device or host allocation failed */
+#define SSS_ECUDA (-3)      /* a CUDA call failed */
+#define SSS_ETIMEOUT (-4)   /* a device wait ran out of iterations */
+#define SSS_ENONFINITE (-5) /* a state became NaN or infinite */
+#define SSS_ENODEVICE (-6)  /* no CUDA device */
+
+/* plan flags */
+#define SSS_RESIDUAL 1u     /* residual arithmetic (accumulate U - I) */
+#define SSS_ROTATING 2u     /* generalised rotating frame */
+
+/* exponential algorithms */
+#define SSS_EXPM_REFERENCE 0 /* first-order Taylor, 4^-R scaling, 2R squarings
+                                (generate_simulator.py:534-578, :706-724) */
+#define SSS_EXPM_TAYLOR 1    /* Taylor of chosen degree, norm-chosen squarings */
+
+typedef struct sss_plan sss_plan;
+
+typedef struct {
+    int N;          /* vectorised dimension */
+    int G;          /* generators: lab frame [L0, Gx, Gy, Gz, Gr] (5),
+                       rotating frame [Gx, Gy, Gz, Gr] (4) */
+    int K;          /* exponentials per step (1, 2, 3, 5, 6) */
+    int Q;          /* Gauss-Legendre nodes (1, 2, 3) */
+    unsigned flags; /* SSS_RESIDUAL | SSS_ROTATING */
+    int expm;       /* SSS_EXPM_REFERENCE or SSS_EXPM_TAYLOR */
+    int quartic_repeats; /* R: 2R squarings in SSS_EXPM_REFERENCE */
+    int taylor_degree;   /* SSS_EXPM_TAYLOR degree (0: chosen per run) */
+} sss_plan_desc;
+
+/* generate_simulator set-up.  generators: G*N*N (lab frame; unused and
+ * may be NULL with SSS_ROTATING, whose per-node generators come from
+ * sss_plan_set_rotating).  weights: K*Q commutator-free weights; nodes: Q
+ * Gauss-Legendre nodes in [0, 1]. */
+int sss_plan_create(sss_plan** plan, const sss_plan_desc* desc,
+                    const double* generators, const double* weights,
+                    const double* nodes);
+
+/* Rotating frame (generate_simulator.py:1567-1677, 901-1021, 1023-1171):
+ * generators_nodes: Q*G*N*N rotating generators at each node offset;
+ * doubles_last: D*2 and singles_last: S, the residual-aware (or plain)
+ * e^{L0 h} blocks for one fine step; V, Vinv: N*N eigenbasis and its
+ * inverse.  2D + S == N.  The fine step h is fixed by these tables: a run
+ * must use the dt/F they were made for. */
+int sss_plan_set_rotating(sss_plan* plan, const double* generators_nodes,
+                          const double* doubles_last, int D,
+                          const double* singles_last, int S, const double* V,
+                          const double* Vinv);
+
+/* Coefficient program of one trajectory: nch channels x nseg segments x 5
+ * doubles (t_end, offset, amplitude, frequency, phase).  A channel's value
+ * at time t is offset + amplitude*cos(tau*frequency*t + phase) for the
+ * first segment with t < t_end, else 0.  Lab frame: coefficient row
+ * [1, ch0, ch1, ch2, ch3]; rotating frame: [ch0, ch1, ch2, ch3]
+ * (superspinsim/generate_generators.py:2317-2358). */
+
+/* simulate() for ntraj independent trajectories, host buffers.
+ *   rho0:  ntraj*N          flattened initial states
+ *   programs: ntraj*nch*nseg*5, or NULL when coeff_table is given
+ *   coeff_table: ntraj*(T*F*Q)*G sampled coefficients in the reference's
+ *          row order (sample t, node k at fine step r in row
+ *          (r*T + t)*Q + k), or NULL
+ *   out:   ntraj*T*N  state after each of the T output samples
+ * Output sample t is at t0 + dt*(t+1); each spans F fine steps of dt/F. */
+int sss_simulate(sss_plan* plan, int ntraj, const double* rho0, int nch,
+                 int nseg, const double* programs, const double* coeff_table,
+                 double t0, double dt, int T, int F, double* out,
+                 void* cuda_stream);
+
+/* The same with every pointer a device pointer. */
+int sss_simulate_device(sss_plan* plan, int ntraj, const double* rho0, int nch,
+                        int nseg, const double* programs,
+                        const double* coeff_table, double t0, double dt, int T,
+                        int F, double* out, void* cuda_stream);
+
+/* Batched sweep: ntraj trajectories, each with its own program, initial
+ * state and number of output samples, run by a persistent kernel that
+ * takes trajectories from a device work queue.  Per output sample t of
+ * trajectory b it writes readout[b*T_max + t] = dot(readout_weights, state)
+ * (a linear functional such as a population or a fluorescence rate); after
+ * its last sample the row is zero-padded.  final_state (ntraj*N) receives
+ * each trajectory's last state (NULL to skip).
+ *   samples: ntraj output-sample counts (NULL: all T_max)
+ *   host != 0: all pointers are host pointers (copied in and out within the
+ *   call); host == 0: device pointers.
+ * Uses SSS_EXPM_TAYLOR arithmetic; lab frame only. */
+int sss_batch_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
+                  int nseg, const double* programs, const int* samples,
+                  double t0, double dt, int T_max, int F,
+                  const double* readout_weights, double* readout,
+                  double* final_state, int host, void* cuda_stream);
+
+/* Kernel launches issued by the last sss_simulate / sss_batch_run call on
+ * this plan (for launch accounting). */
+int sss_plan_last_launches(const sss_plan* plan);
+
+/* Batched-kernel configuration (the autotuner's knobs): lanes per
+ * trajectory (1, 2, 4, 8, 16, 32; 0 = automatic) and CTA size (a multiple
+ * of 32 up to 256; 0 = 128).  No reference counterpart (the reference's
+ * launch shapes are fixed, generate_simulator.py:85-106). */
+int sss_plan_set_batch_config(sss_plan* plan, int lanes, int cta_threads);
+
+/* What the last sss_batch_run used: lanes per trajectory, Taylor degree,
+ * sub-steps per exponential, state rows kept after the reachability
+ * pruning, non-zeros of the pruned pattern, and the kernel's device time in
+ * ms (CUDA events on the launch stream; waits for it).  Any pointer may be
+ * NULL. */
+int sss_plan_batch_info(const sss_plan* plan, int* lanes, int* degree,
+                        int* substeps, int* rows, int* nnz, double* kernel_ms);
+
+/* Measurement utility (no reference counterpart): FP64 FMA throughput of
+ * the current device in TFLOP/s, from a bounded DFMA loop (8 independent
+ * chains per thread, 4 CTAs of 256 threads per SM).  The roofline
+ * denominator of the FP64-bound kernels. */
+int sss_fp64_peak(double* tflops, void* cuda_stream);
+
+const char* sss_last_error(void);
+void sss_plan_destroy(sss_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SSS_H */

@@ -1,0 +1,225 @@
+"""ctypes binding of libsss.so (include/sss.h).
+
+The library is the only compute path of this package: if it is missing or
+cannot be loaded, or no CUDA device is present, calls fail loudly -- there
+is no CPU fallback.
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libsss.so")
+
+SSS_RESIDUAL = 1
+SSS_ROTATING = 2
+SSS_EXPM_REFERENCE = 0
+SSS_EXPM_TAYLOR = 1
+
+ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
+          -5: "ENONFINITE", -6: "ENODEVICE"}
+
+SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
+           "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
+           "sss_plan_set_batch_config", "sss_plan_batch_info",
+           "sss_fp64_peak", "sss_last_error", "sss_plan_destroy"]
+
+
+class SSSError(RuntimeError):
+    """An error code returned by libsss.so."""
+
+    def __init__(self, code, message):
+        super().__init__(f"libsss {ERRORS.get(code, code)}: {message}")
+        self.code = code
+
+
+class PlanDesc(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("G", ctypes.c_int), ("K", ctypes.c_int),
+                ("Q", ctypes.c_int), ("flags", ctypes.c_uint),
+                ("expm", ctypes.c_int), ("quartic_repeats", ctypes.c_int),
+                ("taylor_degree", ctypes.c_int)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(build_if_missing=True):
+    """Load libsss.so (building it in-tree with nvcc if it is absent)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            if not build_if_missing:
+                raise RuntimeError(f"{LIB_PATH} is missing; run "
+                                   "superspinsim_gb300.build.build()")
+            from superspinsim_gb300 import build
+            build.build()
+        L = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        vp = ctypes.c_void_p
+        i, d = ctypes.c_int, ctypes.c_double
+        L.sss_plan_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(PlanDesc),
+                                      dp, dp, dp]
+        L.sss_plan_set_rotating.argtypes = [vp, dp, dp, i, dp, i, dp, dp]
+        sim = [vp, i, dp, i, i, dp, dp, d, d, i, i, dp, vp]
+        L.sss_simulate.argtypes = sim
+        L.sss_simulate_device.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, vp, vp]
+        L.sss_batch_run.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, dp, vp, vp, i, vp]
+        L.sss_plan_last_launches.argtypes = [vp]
+        L.sss_plan_set_batch_config.argtypes = [vp, i, i]
+        L.sss_plan_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, dp]
+        L.sss_fp64_peak.argtypes = [dp, vp]
+        L.sss_fp64_peak.restype = i
+        L.sss_last_error.restype = ctypes.c_char_p
+        L.sss_plan_destroy.argtypes = [vp]
+        L.sss_plan_destroy.restype = None
+        for name in ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
+                     "sss_simulate_device", "sss_batch_run",
+                     "sss_plan_last_launches", "sss_plan_set_batch_config",
+                     "sss_plan_batch_info"]:
+            getattr(L, name).restype = i
+        _lib = L
+        return L
+
+
+def check(code):
+    if code != 0:
+        msg = load().sss_last_error().decode(errors="replace")
+        raise SSSError(code, msg)
+
+
+def dptr(a):
+    """Pointer to a C-contiguous float64 numpy array (or None)."""
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def iptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Plan:
+    """Owner of one sss_plan (device copies of generators and tables)."""
+
+    def __init__(self, generators, weights, nodes, *, residual=True,
+                 expm=SSS_EXPM_TAYLOR, quartic_repeats=35, taylor_degree=0,
+                 rotating=None):
+        L = load()
+        weights = np.ascontiguousarray(weights, dtype=np.float64)
+        nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        K, Q = weights.shape
+        flags = SSS_RESIDUAL if residual else 0
+        if rotating is not None:
+            flags |= SSS_ROTATING
+            gn = np.ascontiguousarray(rotating["generators_nodes"], dtype=np.float64)
+            Qg, G, N, _ = gn.shape
+            assert Qg == Q
+            gens = None
+        else:
+            gens = np.ascontiguousarray(generators, dtype=np.float64)
+            G, N, _ = gens.shape
+        self.N, self.G, self.K, self.Q = N, G, K, Q
+        desc = PlanDesc(N, G, K, Q, flags, expm, quartic_repeats, taylor_degree)
+        h = ctypes.c_void_p()
+        check(L.sss_plan_create(ctypes.byref(h), ctypes.byref(desc), dptr(gens),
+                                dptr(weights), dptr(nodes)))
+        self._h = h
+        if rotating is not None:
+            dl = np.ascontiguousarray(rotating["doubles_last"], dtype=np.float64).reshape(-1, 2)
+            sl = np.ascontiguousarray(rotating["singles_last"], dtype=np.float64)
+            V = np.ascontiguousarray(rotating["vectors_real"], dtype=np.float64)
+            Vi = np.ascontiguousarray(rotating["inv_vectors_real"], dtype=np.float64)
+            check(L.sss_plan_set_rotating(h, dptr(gn), dptr(dl), dl.shape[0], dptr(sl),
+                                          sl.size, dptr(V), dptr(Vi)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.sss_plan_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def simulate(self, rho0, programs, t0, dt, T, F, table=None, stream=None):
+        """rho0 (B, N); programs (B, nch, nseg, 5) or None with table
+        (B, F*T*Q, G).  Returns (B, T, N)."""
+        rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
+        B = rho0.shape[0]
+        out = np.empty((B, T, self.N))
+        if programs is not None:
+            programs = np.ascontiguousarray(programs, dtype=np.float64)
+            nch, nseg = programs.shape[1], programs.shape[2]
+        else:
+            nch = nseg = 0
+        if table is not None:
+            table = np.ascontiguousarray(table, dtype=np.float64)
+        check(load().sss_simulate(self._h, B, dptr(rho0), nch, nseg, dptr(programs),
+                                  dptr(table), float(t0), float(dt), int(T), int(F),
+                                  dptr(out), stream))
+        return out
+
+    def batch(self, rho0, programs, t0, dt, T_max, F, samples=None,
+              readout_weights=None, want_final=False, stream=None):
+        """Host-buffer batched run.  Returns (readout (B, T_max) or None,
+        final (B, N) or None)."""
+        rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
+        programs = np.ascontiguousarray(programs, dtype=np.float64)
+        B = rho0.shape[0]
+        nch, nseg = programs.shape[1], programs.shape[2]
+        ro = np.empty((B, T_max)) if readout_weights is not None else None
+        fin = np.empty((B, self.N)) if want_final else None
+        rw = None if readout_weights is None else np.ascontiguousarray(
+            readout_weights, dtype=np.float64)
+        smp = None if samples is None else np.ascontiguousarray(samples, dtype=np.int32)
+        check(load().sss_batch_run(
+            self._h, B, rho0.ctypes.data_as(ctypes.c_void_p), nch, nseg,
+            programs.ctypes.data_as(ctypes.c_void_p), iptr(smp), float(t0), float(dt),
+            int(T_max), int(F), dptr(rw),
+            None if ro is None else ro.ctypes.data_as(ctypes.c_void_p),
+            None if fin is None else fin.ctypes.data_as(ctypes.c_void_p), 1, stream))
+        return ro, fin
+
+    def batch_device(self, rho0_ptr, B, programs_ptr, nch, nseg, t0, dt, T_max,
+                     F, samples_ptr=None, readout_weights=None, readout_ptr=None,
+                     final_ptr=None, stream=None):
+        """Device-pointer batched run (pointers as integers)."""
+        rw = None if readout_weights is None else np.ascontiguousarray(
+            readout_weights, dtype=np.float64)
+        check(load().sss_batch_run(self._h, B, rho0_ptr, nch, nseg, programs_ptr,
+                                   samples_ptr, float(t0), float(dt), int(T_max),
+                                   int(F), dptr(rw), readout_ptr, final_ptr, 0, stream))
+
+    def set_batch_config(self, lanes=0, cta_threads=0):
+        check(load().sss_plan_set_batch_config(self._h, int(lanes), int(cta_threads)))
+
+    def batch_info(self):
+        vals = [ctypes.c_int() for _ in range(5)]
+        ms = ctypes.c_double()
+        check(load().sss_plan_batch_info(self._h, *[ctypes.byref(v) for v in vals],
+                                         ctypes.byref(ms)))
+        out = dict(zip(["lanes", "degree", "substeps", "rows", "nnz"],
+                       [v.value for v in vals]))
+        out["kernel_ms"] = ms.value
+        return out
+
+    def last_launches(self):
+        return load().sss_plan_last_launches(self._h)
+
+
+def fp64_peak_tflops(stream=None):
+    """Measured FP64 FMA throughput of the current GPU (TFLOP/s)."""
+    v = ctypes.c_double()
+    check(load().sss_fp64_peak(ctypes.byref(v), stream))
+    return v.value

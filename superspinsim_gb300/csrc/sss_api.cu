@@ -1,0 +1,395 @@
+// C-ABI entry points of libsss.so (declared in include/sss.h): plan
+// set-up (the reference's generate_simulator set-up,
+// superspinsim/generate_simulator.py:49-154 and :1683-1814), argument
+// checking, host<->device staging, and dispatch to the plain and batched
+// paths.  No exception or abort crosses the ABI.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+
+#include "sss_internal.cuh"
+
+namespace sss {
+
+static thread_local std::string g_error;
+
+void set_error(const std::string& msg) { g_error = msg; }
+
+int fail(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_error = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return SSS_ENOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return SSS_ENODEVICE;
+    return SSS_ECUDA;
+}
+
+int DevBuf::ensure(size_t n) {
+    if (n <= bytes && p) return SSS_OK;
+    release();
+    if (n == 0) return SSS_OK;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        bytes = 0;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    bytes = n;
+    return SSS_OK;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+static int upload(DevBuf& buf, const double* h, size_t n) {
+    if (int rc = buf.ensure(n * sizeof(double))) return rc;
+    if (n) SSS_CUDA(cudaMemcpy(buf.p, h, n * sizeof(double), cudaMemcpyHostToDevice));
+    return SSS_OK;
+}
+
+static bool finite_all(const double* a, size_t n) {
+    for (size_t i = 0; i < n; i++)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+}  // namespace sss
+
+using namespace sss;
+
+extern "C" {
+
+const char* sss_last_error(void) { return g_error.c_str(); }
+
+int sss_plan_create(sss_plan** out, const sss_plan_desc* d, const double* generators,
+                    const double* weights, const double* nodes) {
+    if (!out || !d) return fail(SSS_EINVAL, "null plan or descriptor");
+    *out = nullptr;
+    if (d->N <= 0 || d->G <= 0 || d->G > kMaxG || d->K <= 0 || d->K > kMaxK || d->Q <= 0 ||
+        d->Q > kMaxQ)
+        return fail(SSS_EINVAL, "bad plan shape (N, G, K, Q)");
+    if (d->expm != SSS_EXPM_REFERENCE && d->expm != SSS_EXPM_TAYLOR)
+        return fail(SSS_EINVAL, "unknown exponential algorithm");
+    if (d->expm == SSS_EXPM_REFERENCE && (d->quartic_repeats < 0 || d->quartic_repeats > 500))
+        return fail(SSS_EINVAL, "quartic_repeats out of range");
+    if (!weights || !nodes) return fail(SSS_EINVAL, "null weights or nodes");
+    bool rotating = (d->flags & SSS_ROTATING) != 0;
+    if (!rotating && !generators) return fail(SSS_EINVAL, "null generators");
+    int dev_count = 0;
+    cudaError_t ce = cudaGetDeviceCount(&dev_count);
+    if (ce != cudaSuccess || dev_count == 0)
+        return fail(SSS_ENODEVICE, std::string("no CUDA device: ") + cudaGetErrorString(ce));
+    sss_plan* p = new (std::nothrow) sss_plan();
+    if (!p) return fail(SSS_ENOMEM, "host allocation failed");
+    p->d = *d;
+    p->rotating = rotating;
+    memcpy(p->W, weights, sizeof(double) * d->K * d->Q);
+    memcpy(p->nodes, nodes, sizeof(double) * d->Q);
+    if (cudaGetDevice(&p->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
+        delete p;
+        return fail(SSS_ECUDA, "cannot query the current device");
+    }
+    size_t NN = (size_t)d->N * d->N;
+    if (!rotating) {
+        p->gens.assign(generators, generators + (size_t)d->G * NN);
+        if (!finite_all(p->gens.data(), p->gens.size())) {
+            delete p;
+            return fail(SSS_ENONFINITE, "generators contain NaN or Inf");
+        }
+        // device layout: generators, then W (K*Q), then nodes (Q)
+        std::vector<double> packed(p->gens);
+        packed.insert(packed.end(), p->W, p->W + d->K * d->Q);
+        packed.insert(packed.end(), p->nodes, p->nodes + d->Q);
+        if (int rc = upload(p->d_gens, packed.data(), packed.size())) {
+            delete p;
+            return rc;
+        }
+        if (int rc = build_sparse(p)) {
+            sss_plan_destroy(p);
+            return rc;
+        }
+    }
+    *out = p;
+    return SSS_OK;
+}
+
+int sss_plan_set_rotating(sss_plan* p, const double* gn, const double* dlast, int D,
+                          const double* slast, int S, const double* V, const double* Vinv) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (!p->rotating) return fail(SSS_EINVAL, "plan was not created with SSS_ROTATING");
+    const int N = p->d.N;
+    if (D < 0 || S < 0 || 2 * D + S != N) return fail(SSS_EINVAL, "2D + S must equal N");
+    if (!gn || !V || !Vinv || (D && !dlast) || (S && !slast))
+        return fail(SSS_EINVAL, "null rotating-frame table");
+    size_t NN = (size_t)N * N;
+    p->gens.assign(gn, gn + (size_t)p->d.Q * p->d.G * NN);
+    std::vector<double> packed(p->gens);
+    packed.insert(packed.end(), p->W, p->W + p->d.K * p->d.Q);
+    packed.insert(packed.end(), p->nodes, p->nodes + p->d.Q);
+    if (int rc = upload(p->d_gens, packed.data(), packed.size())) return rc;
+    p->D = D;
+    p->S = S;
+    p->dlast.assign(dlast, dlast + 2 * (size_t)D);
+    p->slast.assign(slast, slast + (size_t)S);
+    p->V.assign(V, V + NN);
+    p->Vinv.assign(Vinv, Vinv + NN);
+    if (int rc = upload(p->d_dlast, p->dlast.data(), p->dlast.size())) return rc;
+    if (int rc = upload(p->d_slast, p->slast.data(), p->slast.size())) return rc;
+    if (int rc = upload(p->d_V, V, NN)) return rc;
+    if (int rc = upload(p->d_Vinv, Vinv, NN)) return rc;
+    return SSS_OK;
+}
+
+static int check_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                     const double* programs, const double* tab, double dt, int T, int F,
+                     const void* out) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (p->rotating && p->D + p->S == 0) return fail(SSS_EINVAL, "rotating tables not set");
+    if (ntraj < 0 || T < 0 || F <= 0) return fail(SSS_EINVAL, "bad ntraj, T or F");
+    if (ntraj == 0 || T == 0) return SSS_OK;
+    if (!rho0 || !out) return fail(SSS_EINVAL, "null rho0 or output");
+    if (!programs && !tab) return fail(SSS_EINVAL, "need a coefficient program or table");
+    if (programs && (nch < 0 || nch > kMaxCh || nseg <= 0))
+        return fail(SSS_EINVAL, "bad program shape");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(SSS_EINVAL, "dt must be positive and finite");
+    return SSS_OK;
+}
+
+static int simulate_impl(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                         const double* programs, const double* tab, double t0, double dt, int T,
+                         int F, double* out, void* stream, bool host) {
+    if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, tab, dt, T, F, out)) return rc;
+    p->last_launches = 0;
+    if (ntraj == 0 || T == 0) return SSS_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int N = p->d.N;
+    const double *d_rho0 = rho0, *d_prog = programs, *d_tab = tab;
+    double* d_out = out;
+    if (host) {
+        size_t nprog = programs ? (size_t)ntraj * nch * nseg * 5 : 0;
+        size_t ntab = tab ? (size_t)ntraj * F * T * p->d.Q * p->d.G : 0;
+        if (programs && !finite_all(programs, nprog) ) {
+            // +-inf segment ends are allowed; NaN is not
+            for (size_t i = 0; i < nprog; i++)
+                if (std::isnan(programs[i])) return fail(SSS_ENONFINITE, "program contains NaN");
+        }
+        if (int rc = p->w_in.ensure(sizeof(double) * ((size_t)ntraj * N + nprog + ntab))) return rc;
+        if (int rc = p->w_out.ensure(sizeof(double) * (size_t)ntraj * T * N)) return rc;
+        double* base = p->w_in.as<double>();
+        SSS_CUDA(cudaMemcpyAsync(base, rho0, sizeof(double) * ntraj * N, cudaMemcpyHostToDevice, st));
+        d_rho0 = base;
+        if (programs) {
+            SSS_CUDA(cudaMemcpyAsync(base + (size_t)ntraj * N, programs, sizeof(double) * nprog,
+                                     cudaMemcpyHostToDevice, st));
+            d_prog = base + (size_t)ntraj * N;
+        }
+        if (tab) {
+            SSS_CUDA(cudaMemcpyAsync(base + (size_t)ntraj * N + nprog, tab, sizeof(double) * ntab,
+                                     cudaMemcpyHostToDevice, st));
+            d_tab = base + (size_t)ntraj * N + nprog;
+        }
+        d_out = p->w_out.as<double>();
+    }
+    int rc = plain_run(p, ntraj, d_rho0, nch, nseg, d_prog, d_tab, t0, dt, T, F, d_out, st);
+    if (rc) return rc;
+    if (host) {
+        SSS_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)ntraj * T * N,
+                                 cudaMemcpyDeviceToHost, st));
+        SSS_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < (size_t)ntraj * T * N; i++)
+            if (!std::isfinite(out[i])) return fail(SSS_ENONFINITE, "state became NaN or Inf");
+    }
+    return SSS_OK;
+}
+
+int sss_simulate(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                 const double* programs, const double* tab, double t0, double dt, int T, int F,
+                 double* out, void* stream) {
+    return simulate_impl(p, ntraj, rho0, nch, nseg, programs, tab, t0, dt, T, F, out, stream, true);
+}
+
+int sss_simulate_device(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                        const double* programs, const double* tab, double t0, double dt, int T,
+                        int F, double* out, void* stream) {
+    return simulate_impl(p, ntraj, rho0, nch, nseg, programs, tab, t0, dt, T, F, out, stream, false);
+}
+
+int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                  const double* programs, const int* samples, double t0, double dt, int T_max,
+                  int F, const double* readout_weights, double* readout, double* final_state,
+                  int host, void* stream) {
+    if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, T_max, F,
+                           readout ? (const void*)readout : (const void*)final_state))
+        return rc;
+    if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
+    if (p->rotating) return fail(SSS_EINVAL, "batched runs support the lab frame only");
+    if (readout && !readout_weights) return fail(SSS_EINVAL, "readout needs readout_weights");
+    p->last_launches = 0;
+    if (ntraj == 0 || T_max == 0) return SSS_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int N = p->d.N;
+    // per-trajectory sample counts (host copy needed for the reachability
+    // analysis and for validation)
+    std::vector<int> h_samples;
+    if (samples) {
+        h_samples.resize(ntraj);
+        if (host) {
+            memcpy(h_samples.data(), samples, sizeof(int) * ntraj);
+        } else {
+            SSS_CUDA(cudaMemcpy(h_samples.data(), samples, sizeof(int) * ntraj, cudaMemcpyDeviceToHost));
+        }
+        for (int b = 0; b < ntraj; b++)
+            if (h_samples[b] < 0 || h_samples[b] > T_max)
+                return fail(SSS_EINVAL, "samples[b] must lie in [0, T_max]");
+    }
+    const double *d_rho0 = rho0, *d_prog = programs;
+    const int* d_samples = samples;
+    double *d_ro = readout, *d_fin = final_state;
+    size_t nprog = (size_t)ntraj * nch * nseg * 5;
+    if (host) {
+        for (size_t i = 0; i < nprog; i++)
+            if (std::isnan(programs[i])) return fail(SSS_ENONFINITE, "program contains NaN");
+        if (int rc = p->w_in.ensure(sizeof(double) * ((size_t)ntraj * N + nprog))) return rc;
+        double* base = p->w_in.as<double>();
+        SSS_CUDA(cudaMemcpyAsync(base, rho0, sizeof(double) * ntraj * N, cudaMemcpyHostToDevice, st));
+        SSS_CUDA(cudaMemcpyAsync(base + (size_t)ntraj * N, programs, sizeof(double) * nprog,
+                                 cudaMemcpyHostToDevice, st));
+        d_rho0 = base;
+        d_prog = base + (size_t)ntraj * N;
+        if (samples) {
+            if (int rc = p->w_samples.ensure(sizeof(int) * ntraj)) return rc;
+            SSS_CUDA(cudaMemcpyAsync(p->w_samples.p, samples, sizeof(int) * ntraj,
+                                     cudaMemcpyHostToDevice, st));
+            d_samples = p->w_samples.as<int>();
+        }
+        if (readout) {
+            if (int rc = p->w_ro.ensure(sizeof(double) * (size_t)ntraj * T_max)) return rc;
+            d_ro = p->w_ro.as<double>();
+        }
+        if (final_state) {
+            if (int rc = p->w_fin.ensure(sizeof(double) * (size_t)ntraj * N)) return rc;
+            d_fin = p->w_fin.as<double>();
+        }
+    }
+    // reachability needs rho0's support on the host
+    std::vector<double> h_rho0((size_t)ntraj * N);
+    if (host) {
+        memcpy(h_rho0.data(), rho0, sizeof(double) * h_rho0.size());
+    } else {
+        SSS_CUDA(cudaMemcpy(h_rho0.data(), rho0, sizeof(double) * h_rho0.size(), cudaMemcpyDeviceToHost));
+    }
+    (void)h_rho0;
+    int rc = batch_run(p, ntraj, d_rho0, nch, nseg, d_prog, d_samples,
+                       samples ? h_samples.data() : nullptr, t0, dt, T_max, F, readout_weights,
+                       d_ro, d_fin, st);
+    if (rc) return rc;
+    if (host) {
+        if (readout)
+            SSS_CUDA(cudaMemcpyAsync(readout, d_ro, sizeof(double) * (size_t)ntraj * T_max,
+                                     cudaMemcpyDeviceToHost, st));
+        if (final_state)
+            SSS_CUDA(cudaMemcpyAsync(final_state, d_fin, sizeof(double) * (size_t)ntraj * N,
+                                     cudaMemcpyDeviceToHost, st));
+        SSS_CUDA(cudaStreamSynchronize(st));
+    }
+    return SSS_OK;
+}
+
+int sss_plan_last_launches(const sss_plan* p) { return p ? p->last_launches : 0; }
+
+// FP64 FMA throughput probe: every thread runs 8 independent DFMA chains.
+static __global__ void k_dfma_peak(double* out, int iters, double a, double b) {
+    double x[8];
+    for (int j = 0; j < 8; j++) x[j] = threadIdx.x * 1e-9 + j;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) x[j] = fma(x[j], a, b);
+    }
+    double s = 0;
+    for (int j = 0; j < 8; j++) s += x[j];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int sss_fp64_peak(double* tflops, void* stream) {
+    if (!tflops) return fail(SSS_EINVAL, "null output");
+    int dev = 0, sms = 0;
+    SSS_CUDA(cudaGetDevice(&dev));
+    SSS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int blocks = sms * 4, threads = 256, iters = 8192;
+    double* buf = nullptr;
+    SSS_CUDA(cudaMalloc(&buf, sizeof(double) * blocks * threads));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_dfma_peak<<<blocks, threads, 0, st>>>(buf, 256, 0.9999999, 1e-7);
+    cudaEventRecord(e0, st);
+    k_dfma_peak<<<blocks, threads, 0, st>>>(buf, iters, 0.9999999, 1e-7);
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, "fp64 peak probe");
+    *tflops = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    return SSS_OK;
+}
+
+int sss_plan_set_batch_config(sss_plan* p, int lanes, int cta_threads) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 &&
+        lanes != 32)
+        return fail(SSS_EINVAL, "lanes must be 0 (automatic) or a power of two up to 32");
+    if (cta_threads != 0 && (cta_threads < 32 || cta_threads > 256 || cta_threads % 32))
+        return fail(SSS_EINVAL, "cta_threads must be 0 or a multiple of 32 in [32, 256]");
+    p->batch_lanes = lanes;
+    p->batch_threads = cta_threads;
+    return SSS_OK;
+}
+
+int sss_plan_batch_info(const sss_plan* p, int* lanes, int* degree, int* substeps, int* rows,
+                        int* nnz, double* kernel_ms) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (kernel_ms) {
+        *kernel_ms = 0.0;
+        if (p->ev_recorded) {
+            float ms = 0.f;
+            SSS_CUDA(cudaEventSynchronize(p->ev_end));
+            SSS_CUDA(cudaEventElapsedTime(&ms, p->ev_begin, p->ev_end));
+            *kernel_ms = ms;
+        }
+    }
+    if (lanes) *lanes = p->last_batch_lanes;
+    if (degree) *degree = p->last_degree;
+    if (substeps) *substeps = p->last_substeps;
+    if (rows) *rows = p->last_rows;
+    if (nnz) *nnz = p->last_nnz;
+    return SSS_OK;
+}
+
+void sss_plan_destroy(sss_plan* p) {
+    if (!p) return;
+    DevBuf* bufs[] = {&p->d_gens, &p->d_dlast, &p->d_slast, &p->d_V, &p->d_Vinv,
+                      &p->d_sp_rowptr, &p->d_sp_col, &p->d_sp_val, &p->d_row_map,
+                      &p->w_prop, &p->w_in, &p->w_out, &p->w_prog, &p->w_tab, &p->w_aux,
+                      &p->w_queue, &p->w_ro, &p->w_fin, &p->w_samples, &p->w_status};
+    for (DevBuf* b : bufs) b->release();
+    if (p->ev_begin) cudaEventDestroy(p->ev_begin);
+    if (p->ev_end) cudaEventDestroy(p->ev_end);
+    delete p;
+}
+
+}  // extern "C"

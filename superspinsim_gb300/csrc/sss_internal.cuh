@@ -1,0 +1,89 @@
+// Internal declarations shared by the translation units of libsss.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "sss.h"
+
+namespace sss {
+
+constexpr double kTau = 6.283185307179586;
+constexpr int kMaxG = 8;      // generators per frame
+constexpr int kMaxQ = 3;      // Gauss-Legendre nodes
+constexpr int kMaxK = 6;      // exponentials per step
+constexpr int kMaxCh = 4;     // coefficient channels
+constexpr int kPlainMaxN = 52;  // dense shared-memory propagator path
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define SSS_CUDA(call)                                      \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return sss::cuda_fail(e_, #call); \
+    } while (0)
+
+// Device buffer that grows on demand and is owned by a plan.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);
+    void release();
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Sparse form of the generators for the batched vector-action kernel:
+// the union pattern of all generators, row-sorted.  For each pattern entry
+// p: row, col, and the G generator values at (row, col).
+struct SparseGenerators {
+    int N = 0, G = 0, nnz = 0;
+    std::vector<int> row_ptr;   // N+1
+    std::vector<int> col;       // nnz
+    std::vector<double> val;    // G*nnz, generator-major
+};
+
+}  // namespace sss
+
+struct sss_plan {
+    sss_plan_desc d{};
+    double W[sss::kMaxK * sss::kMaxQ] = {};
+    double nodes[sss::kMaxQ] = {};
+    bool rotating = false;
+    int D = 0, S = 0;
+    // host copies
+    std::vector<double> gens;        // lab G*N*N, or rotating Q*G*N*N
+    std::vector<double> dlast, slast, V, Vinv;
+    sss::SparseGenerators sparse;    // lab frame, for sss_batch_run
+    // device copies
+    sss::DevBuf d_gens, d_dlast, d_slast, d_V, d_Vinv;
+    sss::DevBuf d_sp_rowptr, d_sp_col, d_sp_val;
+    sss::DevBuf d_row_map;
+    // workspace
+    sss::DevBuf w_prop, w_in, w_out, w_prog, w_tab, w_aux, w_queue, w_ro,
+        w_fin, w_samples, w_status;
+    int last_launches = 0;
+    int batch_lanes = 0;    // 0: chosen per run
+    int batch_threads = 0;  // CTA size of the batched kernel, 0: 128
+    int last_batch_lanes = 0, last_degree = 0, last_substeps = 0, last_rows = 0,
+        last_nnz = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // around the last batched kernel
+    bool ev_recorded = false;
+};
+
+namespace sss {
+// sss_plain.cu
+int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+              const double* d_prog, const double* d_tab, double t0, double dt,
+              int T, int F, double* d_out, cudaStream_t st);
+// sss_batch.cu
+int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+              const double* d_prog, const int* d_samples, const int* h_samples,
+              double t0, double dt, int T_max, int F, const double* h_rw,
+              double* d_readout, double* d_final, cudaStream_t st);
+int build_sparse(sss_plan* p);
+}  // namespace sss

@@ -1,0 +1,372 @@
+// Plain per-trajectory path: the drop-in for `simulate`
+// (reference superspinsim/generate_simulator.py:1508-2200).
+//
+// The reference builds one step propagator per output sample, all samples
+// in parallel (its only parallel axis), by F serial fine steps of K
+// exponentials each, then chains them serially on the host with 2(T-1)
+// launches and applies the cumulative propagators to rho0.  Here:
+//
+//  k_step_propagators: one CTA per (trajectory, output sample).  The N x N
+//    working set (exponent, Taylor powers, exponential, accumulated step
+//    propagator) lives in shared memory for the whole F x K fine-step loop;
+//    generators stream from L2.  The exponential is either the reference's
+//    own scheme (first-order Taylor after 4^-R scaling, 2R squarings; exact
+//    operation order of :534-578, :706-724) or a degree-12 Taylor
+//    polynomial (Paterson-Stockmeyer, 5 products) after norm-chosen
+//    scaling, in residual form.
+//  k_chain: one CTA per trajectory applies the T step propagators to the
+//    state in order (v <- v + S_t v), an O(T N^2) serial tail instead of the
+//    reference's O(T N^3) chain of matrix products, and writes the state
+//    after every sample (mapped back from the rotating eigenbasis if used).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "sss_device.cuh"
+#include "sss_internal.cuh"
+
+namespace sss {
+namespace {
+
+constexpr int kPlainThreads = 256;
+
+// C = A*B + ca*A + cb*B  (C must alias neither A nor B)
+__device__ void mm(double* __restrict__ C, const double* __restrict__ A,
+                   const double* __restrict__ B, int N, double ca, double cb) {
+    for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
+        int i = idx / N, j = idx - i * N;
+        double acc = ca * A[idx] + cb * B[idx];
+        const double* a = A + i * N;
+#pragma unroll 4
+        for (int k = 0; k < N; k++) acc = fma(a[k], B[k * N + j], acc);
+        C[idx] = acc;
+    }
+}
+
+// Reference order products (generate_simulator.py:706-743): the running
+// sum starts at (2*in) or (L + R) and adds the products k = 0..N-1.
+__device__ void mm_ref(double* __restrict__ C, const double* __restrict__ A,
+                       const double* __restrict__ B, int N, bool square,
+                       bool residual) {
+    for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
+        int i = idx / N, j = idx - i * N;
+        double acc = 0.0;
+        if (residual) acc = square ? 2 * A[idx] : A[idx] + B[idx];
+        for (int k = 0; k < N; k++) acc = fma(A[i * N + k], B[k * N + j], acc);
+        C[idx] = acc;
+    }
+}
+
+struct PlainArgs {
+    int N, G, K, Q, F, T, nch, nseg, expm, R;
+    int t_offset;  // global index of this launch's first output sample
+    bool residual, rotating;
+    const double* gens;   // G*N*N or Q*G*N*N
+    const double* W;      // K*Q (device)
+    const double* nodes;  // Q
+    const double* dlast;  // D*2
+    const double* slast;  // S
+    int D, S;
+    const double* prog;   // ntraj*nch*nseg*5
+    const double* tab;    // ntraj*(F*T*Q)*G
+    double t0, dt;
+    double* out;          // ntraj*T*N*N
+};
+
+__global__ void __launch_bounds__(kPlainThreads)
+k_step_propagators(PlainArgs a) {
+    extern __shared__ double sm[];
+    const int N = a.N, NN = N * N;
+    const int t = blockIdx.x, b = blockIdx.y;
+    double* X = sm;
+    double* X2 = X + NN;
+    double* X3 = X2 + NN;
+    double* X4 = X3 + NN;
+    double* Bm = X4 + NN;
+    double* E = Bm + NN;
+    double* TE = E + NN;
+    double* T2 = TE + NN;
+    __shared__ double coef[kMaxQ * kMaxG];
+    __shared__ double colsum[64];
+    const double h = a.dt / a.F;
+    const double* prog = a.prog ? a.prog + (size_t)b * a.nch * a.nseg * 5 : nullptr;
+
+    for (int i = threadIdx.x; i < NN; i += blockDim.x)
+        TE[i] = (!a.residual && (i / N == i % N)) ? 1.0 : 0.0;
+
+    for (int r = 0; r < a.F; r++) {
+        __syncthreads();
+        if (threadIdx.x < a.Q * a.G) {
+            int k = threadIdx.x / a.G, g = threadIdx.x - k * a.G;
+            double v;
+            if (a.tab) {
+                v = a.tab[(((size_t)b * a.F + r) * a.T + t) * a.Q * a.G + threadIdx.x];
+            } else {
+                double tn = node_time(a.t0, a.dt, a.F, r, a.t_offset + t, a.nodes[k]);
+                if (!a.rotating)
+                    v = (g == 0) ? 1.0 : (g - 1 < a.nch ? channel_value(prog, a.nseg, g - 1, tn) : 0.0);
+                else
+                    v = g < a.nch ? channel_value(prog, a.nseg, g, tn) : 0.0;
+            }
+            coef[k * a.G + g] = v;
+        }
+        __syncthreads();
+        for (int e = a.K - 1; e >= 0; e--) {
+            // exponent (generate_simulator.py:354-448 lab, :450-532 rotating)
+            double wc[kMaxG];
+            if (!a.rotating) {
+                for (int g = 0; g < a.G; g++) {
+                    double acc = 0.0;
+                    for (int k = 0; k < a.Q; k++) acc = fma(a.W[e * a.Q + k], coef[k * a.G + g], acc);
+                    wc[g] = acc;
+                }
+            }
+            for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) {
+                double acc = 0.0;
+                if (!a.rotating) {
+                    for (int g = 0; g < a.G; g++) acc = fma(wc[g], __ldg(a.gens + (size_t)g * NN + idx), acc);
+                    acc *= h;
+                } else {
+                    for (int k = 0; k < a.Q; k++) {
+                        double m1 = h * a.W[e * a.Q + k];
+                        for (int g = 0; g < a.G; g++)
+                            acc = fma(__ldg(a.gens + ((size_t)k * a.G + g) * NN + idx) * coef[k * a.G + g], m1, acc);
+                    }
+                }
+                X[idx] = acc;
+            }
+            __syncthreads();
+            double* Eout;  // the exponential (residual form if a.residual)
+            if (a.expm == SSS_EXPM_REFERENCE) {
+                // :534-578 scale and (non-residual) shift; :882-897 squarings
+                double scale = ldexp(1.0, 2 * a.R);
+                for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) {
+                    double v = X[idx] / scale;
+                    if (!a.residual && idx / N == idx % N) v += 1.0;
+                    X[idx] = v;
+                }
+                __syncthreads();
+                for (int q = 0; q < a.R; q++) {
+                    mm_ref(X2, X, X, N, true, a.residual);
+                    __syncthreads();
+                    mm_ref(X, X2, X2, N, true, a.residual);
+                    __syncthreads();
+                }
+                Eout = X;
+            } else {
+                // scaling: ||X||_1 <= 0.25 * 2^s  (Taylor-12 truncation < 1e-18)
+                if (threadIdx.x < N) {
+                    double s = 0.0;
+                    for (int i = 0; i < N; i++) s += fabs(X[i * N + threadIdx.x]);
+                    colsum[threadIdx.x] = s;
+                }
+                __syncthreads();
+                double nrm = 0.0;
+                for (int j = 0; j < N; j++) nrm = fmax(nrm, colsum[j]);
+                int s = 0;
+                while (nrm > 0.25 && s < 60) { nrm *= 0.5; s++; }
+                if (s > 0) {
+                    double f = ldexp(1.0, -s);
+                    for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) X[idx] *= f;
+                    __syncthreads();
+                }
+                // Paterson-Stockmeyer, E = sum_{j=1..12} X^j/j!
+                const double c[13] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720,
+                                      1.0 / 5040, 1.0 / 40320, 1.0 / 362880, 1.0 / 3628800,
+                                      1.0 / 39916800, 1.0 / 479001600};
+                mm(X2, X, X, N, 0, 0);
+                __syncthreads();
+                mm(X3, X2, X, N, 0, 0);
+                mm(X4, X2, X2, N, 0, 0);
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < NN; idx += blockDim.x)
+                    Bm[idx] = (idx / N == idx % N ? c[8] : 0.0) + c[9] * X[idx] + c[10] * X2[idx] +
+                              c[11] * X3[idx] + c[12] * X4[idx];
+                __syncthreads();
+                mm(E, X4, Bm, N, 0, 0);
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < NN; idx += blockDim.x)
+                    E[idx] += (idx / N == idx % N ? c[4] : 0.0) + c[5] * X[idx] + c[6] * X2[idx] +
+                              c[7] * X3[idx];
+                __syncthreads();
+                mm(Bm, X4, E, N, 0, 0);
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < NN; idx += blockDim.x)
+                    Bm[idx] += c[1] * X[idx] + c[2] * X2[idx] + c[3] * X3[idx];
+                __syncthreads();
+                double* cur = Bm;
+                double* nxt = E;
+                for (int q = 0; q < s; q++) {  // residual squaring: 2E + E^2
+                    mm(nxt, cur, cur, N, 2.0, 0.0);
+                    __syncthreads();
+                    double* tmp = cur; cur = nxt; nxt = tmp;
+                }
+                if (!a.residual) {
+                    for (int idx = threadIdx.x; idx < NN; idx += blockDim.x)
+                        if (idx / N == idx % N) cur[idx] += 1.0;
+                    __syncthreads();
+                }
+                Eout = cur;
+            }
+            // TE <- E (*) TE  (:726-743, :1259-1294)
+            if (a.expm == SSS_EXPM_REFERENCE)
+                mm_ref(T2, Eout, TE, N, false, a.residual);
+            else
+                mm(T2, Eout, TE, N, a.residual ? 1.0 : 0.0, a.residual ? 1.0 : 0.0);
+            __syncthreads();
+            double* tmp = TE; TE = T2; T2 = tmp;
+        }
+        if (a.rotating) {
+            // :901-964 -- TE <- e^{L0 h} TE with residual-aware blocks
+            for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) {
+                int y = idx / N, x = idx - y * N;
+                double v;
+                if (y < 2 * a.D) {
+                    int blk = y >> 1;
+                    double p = a.dlast[2 * blk], q = a.dlast[2 * blk + 1];
+                    double re_in = TE[(2 * blk) * N + x], im_in = TE[(2 * blk + 1) * N + x];
+                    if (a.residual) {
+                        if ((y & 1) == 0) {
+                            v = (1 + p) * re_in - q * im_in;
+                            if (x == 2 * blk) v += p;
+                            if (x == 2 * blk + 1) v -= q;
+                        } else {
+                            v = q * re_in + (1 + p) * im_in;
+                            if (x == 2 * blk) v += q;
+                            if (x == 2 * blk + 1) v += p;
+                        }
+                    } else {
+                        v = ((y & 1) == 0) ? p * re_in - q * im_in : q * re_in + p * im_in;
+                    }
+                } else {
+                    double s = a.slast[y - 2 * a.D];
+                    if (a.residual) {
+                        v = (1 + s) * TE[idx];
+                        if (y == x) v += s;
+                    } else {
+                        v = s * TE[idx];
+                    }
+                }
+                T2[idx] = v;
+            }
+            __syncthreads();
+            double* tmp = TE; TE = T2; T2 = tmp;
+        }
+    }
+    __syncthreads();
+    double* dst = a.out + ((size_t)b * a.T + t) * NN;
+    for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) dst[idx] = TE[idx];
+}
+
+// v <- v + S v (residual) or S v, for t = 0..T-1; writes out[b][t] (lab basis)
+__global__ void __launch_bounds__(kPlainThreads)
+k_chain(const double* __restrict__ S, const double* __restrict__ rho0, const double* __restrict__ V,
+        const double* __restrict__ Vinv, int N, int T, int residual, int t_begin,
+        double* __restrict__ state, double* __restrict__ out) {
+    __shared__ double v[kPlainMaxN], w[kPlainMaxN];
+    const int b = blockIdx.x, NN = N * N;
+    // state[b] holds the chain's running vector between chunks (in the
+    // eigenbasis when rotating)
+    if (t_begin == 0) {
+        if (threadIdx.x < N) {
+            double acc = 0.0;
+            if (Vinv) {
+                for (int k = 0; k < N; k++) acc = fma(Vinv[threadIdx.x * N + k], rho0[(size_t)b * N + k], acc);
+            } else {
+                acc = rho0[(size_t)b * N + threadIdx.x];
+            }
+            v[threadIdx.x] = acc;
+        }
+    } else if (threadIdx.x < N) {
+        v[threadIdx.x] = state[(size_t)b * N + threadIdx.x];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int t = 0; t < T; t++) {
+        const double* St = S + ((size_t)b * T + t) * NN;
+        for (int i = warp; i < N; i += nw) {
+            double acc = 0.0;
+            for (int k = lane; k < N; k += 32) acc = fma(__ldg(St + i * N + k), v[k], acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) w[i] = residual ? v[i] + acc : acc;
+        }
+        __syncthreads();
+        if (threadIdx.x < N) v[threadIdx.x] = w[threadIdx.x];
+        __syncthreads();
+        if (threadIdx.x < N) {
+            double o = v[threadIdx.x];
+            if (V) {
+                o = 0.0;
+                for (int k = 0; k < N; k++) o = fma(V[threadIdx.x * N + k], v[k], o);
+            }
+            out[(size_t)(t_begin + t) * N + threadIdx.x] = o;
+        }
+    }
+    if (threadIdx.x < N) state[(size_t)b * N + threadIdx.x] = v[threadIdx.x];
+}
+
+}  // namespace
+
+int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+              const double* d_prog, const double* d_tab, double t0, double dt,
+              int T, int F, double* d_out, cudaStream_t st) {
+    const int N = p->d.N;
+    if (N > kPlainMaxN)
+        return fail(SSS_EINVAL, "plain path supports N <= 52 (got " + std::to_string(N) + ")");
+    const size_t NN = (size_t)N * N;
+    // Chunk the samples so the step-propagator buffer stays under ~2 GiB.
+    size_t per_sample = NN * sizeof(double);
+    int chunk = (int)std::min<size_t>((size_t)T, std::max<size_t>(1, (2ull << 30) / per_sample));
+    if (int rc = p->w_prop.ensure(per_sample * (size_t)chunk)) return rc;
+    if (int rc = p->w_aux.ensure(sizeof(double) * (size_t)N)) return rc;
+    size_t smem = 8 * NN * sizeof(double);
+    SSS_CUDA(cudaFuncSetAttribute(k_step_propagators, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    int launches = 0;
+    for (int b = 0; b < ntraj; b++) {
+        for (int t_begin = 0; t_begin < T; t_begin += chunk) {
+            int Tc = std::min(chunk, T - t_begin);
+            PlainArgs a{};
+            a.N = N; a.G = p->d.G; a.K = p->d.K; a.Q = p->d.Q; a.F = F; a.T = Tc;
+            a.nch = nch; a.nseg = nseg; a.expm = p->d.expm; a.R = p->d.quartic_repeats;
+            a.residual = (p->d.flags & SSS_RESIDUAL) != 0;
+            a.rotating = p->rotating;
+            a.gens = p->d_gens.as<double>();
+            a.W = p->d_gens.as<double>() + p->gens.size();  // W and nodes follow the generators
+            a.nodes = a.W + p->d.K * p->d.Q;
+            a.dlast = p->d_dlast.as<double>(); a.slast = p->d_slast.as<double>();
+            a.D = p->D; a.S = p->S;
+            a.prog = d_prog ? d_prog + (size_t)b * nch * nseg * 5 : nullptr;
+            a.tab = nullptr;
+            a.t0 = t0;
+            a.dt = dt;
+            a.t_offset = t_begin;
+            a.out = p->w_prop.as<double>();
+            if (d_tab) {
+                // copy this chunk's rows (r, t, k) of the table, in order
+                size_t rowG = (size_t)p->d.Q * p->d.G;
+                if (int rc = p->w_tab.ensure(sizeof(double) * (size_t)F * Tc * rowG)) return rc;
+                const double* src = d_tab + (size_t)b * F * T * rowG;
+                SSS_CUDA(cudaMemcpy2DAsync(p->w_tab.p, Tc * rowG * sizeof(double),
+                                           src + (size_t)t_begin * rowG, (size_t)T * rowG * sizeof(double),
+                                           Tc * rowG * sizeof(double), F, cudaMemcpyDeviceToDevice, st));
+                a.tab = p->w_tab.as<double>();
+            }
+            dim3 grid(Tc, 1);
+            k_step_propagators<<<grid, kPlainThreads, smem, st>>>(a);
+            launches++;
+            SSS_CUDA(cudaGetLastError());
+            const double* V = p->rotating ? p->d_V.as<double>() : nullptr;
+            const double* Vi = p->rotating ? p->d_Vinv.as<double>() : nullptr;
+            k_chain<<<1, kPlainThreads, 0, st>>>(p->w_prop.as<double>(), d_rho0 + (size_t)b * N, V, Vi,
+                                                 N, Tc, a.residual ? 1 : 0, t_begin,
+                                                 p->w_aux.as<double>(), d_out + (size_t)b * T * N);
+            launches++;
+            SSS_CUDA(cudaGetLastError());
+        }
+    }
+    p->last_launches = launches;
+    return SSS_OK;
+}
+
+}  // namespace sss

