@@ -229,6 +229,8 @@ def main():
     ap.add_argument("--n-freq", type=int, default=N_FREQ)
     ap.add_argument("--duration", type=float, default=DURATION)
     ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     rank, world = dist_setup()
@@ -250,7 +252,7 @@ def main():
     rho0 = np.repeat(flatten_density(rho, N, vm)[None], B, axis=0)
     w = population_weights(vm, [3, 4, 5])
     sweep = Sweep(gens, vm, number_of_exponentials=K_EXP, number_of_fine_divisions=F,
-                  lanes=args.lanes)
+                  lanes=args.lanes, cta_threads=args.threads, variant=args.variant)
     plan = sweep.plan
 
     stream = torch.cuda.Stream()
@@ -293,7 +295,7 @@ def main():
 
     # e2e: public API, host buffers in and out, every step
     e2e_times = []
-    for i in range(args.warmup + args.steps):
+    for i in range(1 + args.steps):  # the plan and kernel are already warm
         torch.cuda.synchronize()
         barrier(world)
         t = time.perf_counter()
@@ -301,7 +303,7 @@ def main():
                         DT_OUT, readout_weights=w)
         fluor = 65.9e6*trapezoid(out["readout"], DT_OUT)
         el = time.perf_counter() - t
-        if i >= args.warmup:
+        if i >= 1:
             e2e_times.append(el)
     e2e_s = max_over_ranks(sum(e2e_times), world)
     e2e_value = B*T*F*world*args.steps/e2e_s

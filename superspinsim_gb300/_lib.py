@@ -71,7 +71,7 @@ def load(build_if_missing=True):
         L.sss_simulate_device.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, vp, vp]
         L.sss_batch_run.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, dp, vp, vp, i, vp]
         L.sss_plan_last_launches.argtypes = [vp]
-        L.sss_plan_set_batch_config.argtypes = [vp, i, i]
+        L.sss_plan_set_batch_config.argtypes = [vp, i, i, i]
         L.sss_plan_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, dp]
         L.sss_fp64_peak.argtypes = [dp, vp]
         L.sss_fp64_peak.restype = i
@@ -201,8 +201,9 @@ class Plan:
                                    samples_ptr, float(t0), float(dt), int(T_max),
                                    int(F), dptr(rw), readout_ptr, final_ptr, 0, stream))
 
-    def set_batch_config(self, lanes=0, cta_threads=0):
-        check(load().sss_plan_set_batch_config(self._h, int(lanes), int(cta_threads)))
+    def set_batch_config(self, lanes=0, cta_threads=0, variant=0):
+        check(load().sss_plan_set_batch_config(self._h, int(lanes), int(cta_threads),
+                                               int(variant)))
 
     def batch_info(self):
         vals = [ctypes.c_int() for _ in range(5)]

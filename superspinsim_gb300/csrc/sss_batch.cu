@@ -9,29 +9,38 @@
 // exponential is applied: instead of forming exp(Omega) as a matrix
 // (2R = 70 dense N x N squarings per exponential in the reference, :706-724
 // and :882-897), its action on the state is summed directly,
-//     v <- v + sum_{j=1..d} Omega^j v / j!   (m sub-steps of Omega/m),
+//     v <- sum_{j=0..d} Omega^j v / j!   (m sub-steps of Omega/m),
 // with d and m chosen from a norm bound so the truncation stays below
 // 1e-18 per exponential.  Omega = h * sum_g a_g G_g is assembled only on
-// the union sparsity pattern of the generators, restricted to the state
-// entries reachable from the initial states' support (entries outside it
-// are exact zeros for all time and are skipped, so results are unchanged).
+// the union sparsity pattern of the generators that are active in the
+// batch (a generator whose coefficient is zero for every trajectory is
+// dropped), restricted to the state entries reachable from the initial
+// states' support: entries outside it are exact zeros for all time, so
+// skipping them changes no result.
 //
-// Layout: a "group" of L lanes (one warp or a fraction of one) owns one
-// trajectory at a time; its rows are split across the L lanes, balanced by
-// non-zeros.  Generator values, the CSR pattern and readout weights are
-// staged in shared memory once per CTA; per-group state (assembled Omega,
-// state vector, Taylor terms, coefficients) lives in shared memory.  Groups
-// take trajectories from a global atomic counter (the device work queue)
-// and keep going until it is exhausted, so uneven trajectory lengths
-// balance across the GPU.  The step loop is flat -- finishing a trajectory
-// and loading the next is a short branch inside it -- so the groups of a
-// warp stay converged in the arithmetic.
+// FP64 on GB300 issues about 2 DFMA per clock per SM with a 75-cycle
+// latency, so the kernel is organised to spend FP64 issue slots only on the
+// sparse products and to keep several independent FMA chains per warp:
+//
+//  * a group of L lanes owns one trajectory; its rows are split across the
+//    L lanes balanced by non-zeros, so a warp instruction carries as many
+//    useful lanes as the row structure allows (an FP64 warp instruction
+//    costs the same issue time however many of its lanes are active);
+//  * the series is evaluated in Horner form, w <- v + (Omega w)/j for
+//    j = d..1, so closing a row costs one FMA; the assembled Omega entries,
+//    packed column/row words and state vectors live in shared memory, whose
+//    loads do not use FP64 issue slots;
+//  * groups take trajectories from a global atomic counter (the device work
+//    queue) until it runs dry, so uneven trajectory lengths balance across
+//    SMs; the step loop is flat (finishing a trajectory and starting the
+//    next is a short branch inside it) so a warp's groups stay converged.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <numeric>
 #include <vector>
 
@@ -41,7 +50,7 @@
 namespace sss {
 
 // ---------------------------------------------------------------------------
-// host: sparse pattern
+// host: sparse pattern of the lab-frame generators
 // ---------------------------------------------------------------------------
 
 int build_sparse(sss_plan* p) {
@@ -74,130 +83,155 @@ namespace {
 constexpr int kMaxTaylor = 24;
 
 struct BatchArgs {
-    int M, G, K, Q, F, nch, nseg, T_max, ntraj, degree, substeps;
-    int nnz;
+    int M;        // state rows kept (reachable)
+    int Ga;       // active generators
+    int K, Q, F, nch, nseg, T_max, ntraj, degree, substeps, N;
+    int E;        // entries per lane (max over lanes)
     double h_sub, t0, dt;
-    const double* toff;      // F: (r*dt)/F, rounded as the reference rounds it
-    const double* noff;      // Q: (dt*node_k)/F
-    const double* W;         // K*Q
-    const double* nodes;     // Q
-    const int* rows;         // M+1 CSR row pointer (compressed, lane-ordered)
-    const int* cols;         // nnz (compressed column index)
-    const double* vals;      // G*nnz
-    const int* lane_rows;    // L+1: rows [lane_rows[l], lane_rows[l+1]) belong to lane l
-    const int* row_orig;     // M: original index of compressed row
-    const double* rw;        // M readout weights (compressed), or null
-    const double* rho0;      // ntraj*N
-    const double* prog;      // ntraj*nch*nseg*5
-    const int* samples;      // ntraj or null
-    int N;
-    double* readout;         // ntraj*T_max or null
-    double* fin;             // ntraj*N or null
-    int* queue;              // work counter
+    int gen_index[kMaxG];      // active generator -> coefficient slot
+    const double* toff;        // F: (r*dt)/F
+    const double* noff;        // Q: (dt*node_k)/F
+    const double* W;           // K*Q
+    const double* gv;          // Ga * E * L  generator values [g][e][l]
+    const unsigned* ent;       // E * L  packed entry words [e][l]
+    const int* lane_rows;      // L: entries of each lane
+    const int* row_orig;       // M
+    const double* rw;          // M readout weights (or null)
+    const double* rho0;        // ntraj*N
+    const double* prog;        // ntraj*nch*nseg*5
+    const int* samples;        // ntraj or null
+    double* readout;           // ntraj*T_max or null
+    double* fin;               // ntraj*N or null
+    int* queue;
     double inv_j[kMaxTaylor + 1];
 };
 
-template <int L>
-__global__ void __launch_bounds__(256) k_batch(const BatchArgs a) {
-    extern __shared__ double smem[];
-    const int M = a.M, nnz = a.nnz, G = a.G;
-    // CTA-shared staging
-    double* s_val = smem;                              // G*nnz
-    double* s_rw = s_val + (size_t)G * nnz;            // M
-    int* s_rows = reinterpret_cast<int*>(s_rw + M);    // M+1
-    int* s_cols = s_rows + (M + 1);                    // nnz
-    int* s_lane = s_cols + nnz;                        // L+1
-    size_t shared_words = (size_t)G * nnz + M + ((M + 1 + nnz + L + 1 + 1) / 2);
-    double* slots = smem + shared_words;
-    const int slot = threadIdx.x / L, li = threadIdx.x % L;
-    const int per_slot = nnz + 4 * M + kMaxQ * kMaxG;
-    double* Om = slots + (size_t)slot * per_slot;
-    double* v = Om + nnz;
-    double* term = v + M;
-    double* nxt = term + M;
-    double* acc = nxt + M;
-    double* coef = acc + M;
+// Entry word: bits 0-15 column (compressed), bits 16-31 (row + 1) when the
+// entry closes its row, else 0.
+__device__ __forceinline__ int ent_col(unsigned w) { return (int)(w & 0xffffu); }
+__device__ __forceinline__ int ent_end(unsigned w) { return (int)(w >> 16); }
 
-    for (int i = threadIdx.x; i < G * nnz; i += blockDim.x) s_val[i] = a.vals[i];
+// Coefficients of the current fine step at the Q nodes, lab frame
+// [1, ch0, ch1, ...] restricted to the active generators.
+__device__ __forceinline__ void sample_coefficients(const BatchArgs& a, const double* prog, int t,
+                                                    int r, int li, int L, double* coef) {
+    for (int i = li; i < a.Q * a.Ga; i += L) {
+        int k = i / a.Ga, g = a.gen_index[i - k * a.Ga];
+        double val = 1.0;
+        if (g > 0) {
+            // ((t0 + (r*dt)/F) + dt*t) + (dt*node)/F, each op rounded
+            double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + r)),
+                                            __dmul_rn(a.dt, (double)t)),
+                                  __ldg(a.noff + k));
+            val = (g - 1 < a.nch) ? channel_value(prog, a.nseg, g - 1, tn) : 0.0;
+        }
+        coef[i] = val;
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
+    extern __shared__ double smem[];
+    const int M = a.M, Ga = a.Ga, E = a.E;
+    const int slot = threadIdx.x / L, li = threadIdx.x % L;
+    // CTA-shared: generator values [g][e][l], entry words [e][l], readout
+    // weights; then per slot: Omega [e][l], v, two Horner buffers, coefs
+    double* s_gv = smem;
+    double* s_rw = s_gv + (size_t)Ga * E * L;
+    unsigned* s_ent = reinterpret_cast<unsigned*>(s_rw + M);
+    const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
+    const size_t per_slot = ((size_t)E * L + 3 * M + kMaxQ * kMaxG) | 1;
+    double* Om = smem + shared_words + slot * per_slot;
+    double* v = Om + (size_t)E * L;
+    double* bufA = v + M;
+    double* bufB = bufA + M;
+    double* coef = bufB + M;
+    int* s_cnt = reinterpret_cast<int*>(s_ent + (size_t)E * L);
+
+    for (int i = threadIdx.x; i < Ga * E * L; i += blockDim.x) s_gv[i] = a.gv[i];
+    for (int i = threadIdx.x; i < E * L; i += blockDim.x) s_ent[i] = a.ent[i];
+    for (int i = threadIdx.x; i < L; i += blockDim.x) s_cnt[i] = a.lane_rows[i];
     for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
-    for (int i = threadIdx.x; i <= M; i += blockDim.x) s_rows[i] = a.rows[i];
-    for (int i = threadIdx.x; i < nnz; i += blockDim.x) s_cols[i] = a.cols[i];
-    for (int i = threadIdx.x; i <= L; i += blockDim.x) s_lane[i] = a.lane_rows[i];
     __syncthreads();
 
     const unsigned lane_in_warp = threadIdx.x & 31;
-    const unsigned gmask = (L == 32) ? 0xffffffffu
-                                     : (((1u << L) - 1u) << (lane_in_warp / L * L));
-    const int r_begin = s_lane[li], r_end = s_lane[li + 1];
-
+    const unsigned leader = lane_in_warp / L * L;
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    const int nE = s_cnt[li];  // entries of this lane
     int b = -1, T_b = 0, t = 0, r = 0;
     const double* prog = nullptr;
-    // Flat loop: one iteration = one fine step of the group's trajectory.
+
     while (true) {
         if (r == 0 && t >= T_b) {
-            // finish the current trajectory, take the next one
-            if (b >= 0 && a.fin) {
-                for (int i = r_begin; i < r_end; i++) a.fin[(size_t)b * a.N + a.row_orig[i]] = v[i];
-            }
+            if (b >= 0 && a.fin)
+                for (int e = 0; e < nE; e++) {
+                    unsigned w = s_ent[e * L + li];
+                    if (ent_end(w)) {
+                        int row = ent_end(w) - 1;
+                        a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                    }
+                }
             int nb = 0;
             if (li == 0) nb = atomicAdd(a.queue, 1);
-            nb = __shfl_sync(gmask, nb, lane_in_warp / L * L);
+            nb = __shfl_sync(gmask, nb, leader);
             b = nb;
             if (b >= a.ntraj) break;
             T_b = a.samples ? a.samples[b] : a.T_max;
             t = 0;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
-            for (int i = r_begin; i < r_end; i++) v[i] = a.rho0[(size_t)b * a.N + a.row_orig[i]];
+            for (int e = 0; e < nE; e++) {
+                unsigned w = s_ent[e * L + li];
+                if (ent_end(w)) {
+                    int row = ent_end(w) - 1;
+                    v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
+                }
+            }
             __syncwarp(gmask);
             if (T_b == 0) continue;
         }
-        // coefficients at the Q nodes: [1, ch0, ch1, ...] (lab frame)
-        for (int i = li; i < a.Q * G; i += L) {
-            int k = i / G, g = i - k * G;
-            double val = 1.0;
-            if (g > 0) {
-                // ((t0 + (r*dt)/F) + dt*t) + (dt*node)/F, each op rounded
-                double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + r)),
-                                                __dmul_rn(a.dt, (double)t)),
-                                      __ldg(a.noff + k));
-                val = (g - 1 < a.nch) ? channel_value(prog, a.nseg, g - 1, tn) : 0.0;
-            }
-            coef[i] = val;
-        }
+        sample_coefficients(a, prog, t, r, li, L, coef);
         __syncwarp(gmask);
-        for (int e = a.K - 1; e >= 0; e--) {
+        for (int e_exp = a.K - 1; e_exp >= 0; e_exp--) {
             double ag[kMaxG];
-            for (int g = 0; g < G; g++) {
+            for (int g = 0; g < Ga; g++) {
                 double s = 0.0;
-                for (int k = 0; k < a.Q; k++) s = fma(a.W[e * a.Q + k], coef[k * G + g], s);
+                for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
                 ag[g] = s * a.h_sub;
             }
-            // assemble Omega on my rows' entries
-            for (int p = s_rows[r_begin]; p < s_rows[r_end]; p++) {
+            // assemble Omega on this lane's entries
+            for (int e = 0; e < nE; e++) {
                 double o = 0.0;
-                for (int g = 0; g < G; g++) o = fma(ag[g], s_val[(size_t)g * nnz + p], o);
-                Om[p] = o;
+                for (int g = 0; g < Ga; g++) o = fma(ag[g], s_gv[((size_t)g * E + e) * L + li], o);
+                Om[e * L + li] = o;
             }
             for (int m = 0; m < a.substeps; m++) {
-                for (int i = r_begin; i < r_end; i++) {
-                    term[i] = v[i];
-                    acc[i] = 0.0;
-                }
-                __syncwarp(gmask);
-                double* cur = term;
-                double* nx = nxt;
-                for (int j = 1; j <= a.degree; j++) {
-                    for (int i = r_begin; i < r_end; i++) {
-                        double s = 0.0;
-                        for (int p = s_rows[i]; p < s_rows[i + 1]; p++) s = fma(Om[p], cur[s_cols[p]], s);
-                        s *= a.inv_j[j];
-                        nx[i] = s;
-                        acc[i] += s;
+                // Horner: w <- v + (Omega w)/j for j = d..1, starting at w = v
+                const double* cur = v;
+                double* nxt = bufA;
+                for (int j = a.degree; j >= 1; j--) {
+                    const double ij = a.inv_j[j];
+                    double s = 0.0;
+                    for (int e = 0; e < nE; e++) {
+                        unsigned w = s_ent[e * L + li];
+                        s = fma(Om[e * L + li], cur[ent_col(w)], s);
+                        if (ent_end(w)) {
+                            int row = ent_end(w) - 1;
+                            nxt[row] = fma(s, ij, v[row]);
+                            s = 0.0;
+                        }
                     }
                     __syncwarp(gmask);
-                    double* tmp = cur; cur = nx; nx = tmp;
+                    cur = nxt;
+                    nxt = (nxt == bufA) ? bufB : bufA;
                 }
-                for (int i = r_begin; i < r_end; i++) v[i] += acc[i];
+                // cur holds exp(Omega) v on every row; copy my rows into v
+                for (int e = 0; e < nE; e++) {
+                    unsigned w = s_ent[e * L + li];
+                    if (ent_end(w)) {
+                        int row = ent_end(w) - 1;
+                        v[row] = cur[row];
+                    }
+                }
                 __syncwarp(gmask);
             }
         }
@@ -205,7 +239,13 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a) {
             r = 0;
             if (a.readout) {
                 double s = 0.0;
-                for (int i = r_begin; i < r_end; i++) s = fma(s_rw[i], v[i], s);
+                for (int e = 0; e < nE; e++) {
+                    unsigned w = s_ent[e * L + li];
+                    if (ent_end(w)) {
+                        int row = ent_end(w) - 1;
+                        s = fma(s_rw[row], v[row], s);
+                    }
+                }
 #pragma unroll
                 for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
                 if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
@@ -215,13 +255,140 @@ __global__ void __launch_bounds__(256) k_batch(const BatchArgs a) {
     }
 }
 
-template <int L>
-int launch_batch(sss_plan* p, const BatchArgs& a, int threads, size_t smem, cudaStream_t st) {
-    SSS_CUDA(cudaFuncSetAttribute(k_batch<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+// Register variant (per-lane entry count <= EPL): the lane's assembled
+// Omega entries and packed words live in registers for the whole step, its
+// rows are padded to an even length and summed in two interleaved chains
+// (merged at the row end), and the unrolled entry loop exits at the lane's
+// own count.  Generator values stay in global memory (read once per
+// exponential, L1-resident).
+template <int L, int EPL>
+__global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
+    extern __shared__ double smem[];
+    const int M = a.M, Ga = a.Ga;
+    const int slot = threadIdx.x / L, li = threadIdx.x % L;
+    const size_t per_slot = (3 * (size_t)M + kMaxQ * kMaxG) | 1;
+    double* v = smem + slot * per_slot;
+    double* bufA = v + M;
+    double* bufB = bufA + M;
+    double* coef = bufB + M;
+    double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
+    for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
+    unsigned ent[EPL];
+#pragma unroll
+    for (int e = 0; e < EPL; e++) ent[e] = __ldg(a.ent + (size_t)e * L + li);
+    const int nE = __ldg(a.lane_rows + li);
+    __syncthreads();
+
+    const unsigned lane_in_warp = threadIdx.x & 31;
+    const unsigned leader = lane_in_warp / L * L;
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    int b = -1, T_b = 0, t = 0, r = 0;
+    const double* prog = nullptr;
+    double om[EPL];
+
+    while (true) {
+        if (r == 0 && t >= T_b) {
+            if (b >= 0 && a.fin) {
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                    }
+            }
+            int nb = 0;
+            if (li == 0) nb = atomicAdd(a.queue, 1);
+            nb = __shfl_sync(gmask, nb, leader);
+            b = nb;
+            if (b >= a.ntraj) break;
+            T_b = a.samples ? a.samples[b] : a.T_max;
+            t = 0;
+            prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
+#pragma unroll
+            for (int e = 0; e < EPL; e++)
+                if (ent_end(ent[e])) {
+                    int row = ent_end(ent[e]) - 1;
+                    v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
+                }
+            __syncwarp(gmask);
+            if (T_b == 0) continue;
+        }
+        sample_coefficients(a, prog, t, r, li, L, coef);
+        __syncwarp(gmask);
+        for (int e_exp = a.K - 1; e_exp >= 0; e_exp--) {
+            double ag[kMaxG];
+            for (int g = 0; g < Ga; g++) {
+                double s = 0.0;
+                for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
+                ag[g] = s * a.h_sub;
+            }
+#pragma unroll
+            for (int e = 0; e < EPL; e++) om[e] = 0.0;
+            for (int g = 0; g < Ga; g++) {
+                const double c = ag[g];
+                if (c == 0.0) continue;
+                const double* gv = a.gv + (size_t)g * EPL * L + li;
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (e < nE) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);
+            }
+            for (int m = 0; m < a.substeps; m++) {
+                const double* cur = v;
+                double* nxt = bufA;
+                for (int j = a.degree; j >= 1; j--) {
+                    const double ij = a.inv_j[j];
+                    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+                    for (int e = 0; e < EPL; e += 2) {
+                        if (e >= nE) break;
+                        s0 = fma(om[e], cur[ent_col(ent[e])], s0);
+                        s1 = fma(om[e + 1], cur[ent_col(ent[e + 1])], s1);
+                        if (ent_end(ent[e + 1])) {
+                            int row = ent_end(ent[e + 1]) - 1;
+                            nxt[row] = fma(s0 + s1, ij, v[row]);
+                            s0 = 0.0;
+                            s1 = 0.0;
+                        }
+                    }
+                    __syncwarp(gmask);
+                    cur = nxt;
+                    nxt = (nxt == bufA) ? bufB : bufA;
+                }
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        v[row] = cur[row];
+                    }
+                __syncwarp(gmask);
+            }
+        }
+        if (++r == a.F) {
+            r = 0;
+            if (a.readout) {
+                double s = 0.0;
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        s = fma(s_rw[row], v[row], s);
+                    }
+#pragma unroll
+                for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+            }
+            t++;
+        }
+    }
+}
+
+template <class Kern>
+int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_per_cta,
+           size_t smem, cudaStream_t st) {
+    SSS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    SSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<L>, threads, smem));
+    SSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
     if (per_sm < 1) return fail(SSS_EINVAL, "batched kernel does not fit on an SM");
-    int slots_per_cta = threads / L;
     int want = (a.ntraj + slots_per_cta - 1) / slots_per_cta;
     int grid = std::max(1, std::min(want, per_sm * p->num_sms));
     if (!p->ev_begin) {
@@ -229,11 +396,23 @@ int launch_batch(sss_plan* p, const BatchArgs& a, int threads, size_t smem, cuda
         SSS_CUDA(cudaEventCreate(&p->ev_end));
     }
     SSS_CUDA(cudaEventRecord(p->ev_begin, st));
-    k_batch<L><<<grid, threads, smem, st>>>(a);
+    kern<<<grid, threads, smem, st>>>(a);
     SSS_CUDA(cudaGetLastError());
     SSS_CUDA(cudaEventRecord(p->ev_end, st));
     p->ev_recorded = true;
+    p->last_grid = grid;
     return SSS_OK;
+}
+
+
+template <int L>
+int launch_reg(sss_plan* p, int epl, const BatchArgs& a, int threads, size_t smem, cudaStream_t st) {
+    switch (epl) {
+        case 8: return launch(p, k_batch_reg<L, 8>, a, threads, threads / L, smem, st);
+        case 16: return launch(p, k_batch_reg<L, 16>, a, threads, threads / L, smem, st);
+        case 32: return launch(p, k_batch_reg<L, 32>, a, threads, threads / L, smem, st);
+        default: return launch(p, k_batch_reg<L, 64>, a, threads, threads / L, smem, st);
+    }
 }
 
 }  // namespace
@@ -276,19 +455,42 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     (void)h_samples;
     const int N = p->d.N, G = p->d.G;
     const SparseGenerators& sp = p->sparse;
-    // ---- reachable rows from the initial states' support ----
-    std::vector<double> h_rho0((size_t)ntraj * N);
-    SSS_CUDA(cudaMemcpyAsync(h_rho0.data(), d_rho0, sizeof(double) * h_rho0.size(), cudaMemcpyDeviceToHost, st));
+    std::vector<double> h_rho0((size_t)ntraj * N), h_prog((size_t)ntraj * nch * nseg * 5);
+    SSS_CUDA(cudaMemcpyAsync(h_rho0.data(), d_rho0, sizeof(double) * h_rho0.size(),
+                             cudaMemcpyDeviceToHost, st));
+    SSS_CUDA(cudaMemcpyAsync(h_prog.data(), d_prog, sizeof(double) * h_prog.size(),
+                             cudaMemcpyDeviceToHost, st));
     SSS_CUDA(cudaStreamSynchronize(st));
+    // ---- active generators: L0 always; channel c drives generator c+1 ----
+    std::vector<double> cmax(G, 0.0);
+    cmax[0] = 1.0;
+    for (int b = 0; b < ntraj; b++)
+        for (int c = 0; c < nch && c + 1 < G; c++)
+            for (int s = 0; s < nseg; s++) {
+                const double* q = &h_prog[(((size_t)b * nch + c) * nseg + s) * 5];
+                if (q[0] == -INFINITY) continue;  // never matches
+                cmax[c + 1] = std::max(cmax[c + 1], std::fabs(q[1]) + std::fabs(q[2]));
+            }
+    std::vector<int> active;
+    for (int g = 0; g < G; g++) {
+        bool nonzero_gen = false;
+        for (int q = 0; q < sp.nnz; q++) nonzero_gen |= sp.val[(size_t)g * sp.nnz + q] != 0.0;
+        if (cmax[g] > 0.0 && nonzero_gen) active.push_back(g);
+    }
+    const int Ga = (int)active.size();
+    // ---- reachable rows from the initial states' support ----
     std::vector<char> reach(N, 0);
     std::vector<int> stack;
     for (int b = 0; b < ntraj; b++)
         for (int i = 0; i < N; i++)
             if (h_rho0[(size_t)b * N + i] != 0.0 && !reach[i]) { reach[i] = 1; stack.push_back(i); }
-    // column c influences row r when (r, c) is in the pattern
     std::vector<std::vector<int>> influences(N);
     for (int r = 0; r < N; r++)
-        for (int q = sp.row_ptr[r]; q < sp.row_ptr[r + 1]; q++) influences[sp.col[q]].push_back(r);
+        for (int q = sp.row_ptr[r]; q < sp.row_ptr[r + 1]; q++) {
+            bool nz = false;
+            for (int g : active) nz |= sp.val[(size_t)g * sp.nnz + q] != 0.0;
+            if (nz) influences[sp.col[q]].push_back(r);
+        }
     while (!stack.empty()) {
         int c = stack.back();
         stack.pop_back();
@@ -301,82 +503,29 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     const int M = (int)rows_reached.size();
     if (d_readout) SSS_CUDA(cudaMemsetAsync(d_readout, 0, sizeof(double) * (size_t)ntraj * T_max, st));
     if (d_final) SSS_CUDA(cudaMemsetAsync(d_final, 0, sizeof(double) * (size_t)ntraj * N, st));
-    if (M == 0) { p->last_launches = 0; return SSS_OK; }
-
-    // ---- lanes per trajectory (autotuned choice comes from the caller's
-    // table; default from the problem size) ----
-    // Lanes per trajectory: FP64 on GB300 issues ~2 DFMA/clk/SM with a
-    // 75-cycle latency, so each SM wants >= 16 warps of dependent chains.
-    // Take the fewest lanes that give that many lanes in flight, capped by
-    // the rows available to split.
-    int L = 1;
-    {
-        const long want = (long)p->num_sms * 16 * 32;
-        int cap = 1;
-        while (cap < 32 && cap * 2 <= std::max(1, M)) cap *= 2;
-        while (L < cap && (long)ntraj * L < want) L *= 2;
-    }
-    if (p->batch_lanes > 0) L = p->batch_lanes;
-    // ---- assign rows to lanes balanced by non-zeros; relabel compressed
-    // rows so that each lane's rows are contiguous ----
-    std::vector<int> nz_of(M);
-    for (int i = 0; i < M; i++) {
-        int r = rows_reached[i], c = 0;
-        for (int q = sp.row_ptr[r]; q < sp.row_ptr[r + 1]; q++) c += reach[sp.col[q]] ? 1 : 0;
-        nz_of[i] = c + 2;  // + per-row overhead
-    }
-    std::vector<int> order(M);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return nz_of[x] > nz_of[y]; });
-    std::vector<long> load(L, 0);
-    std::vector<std::vector<int>> lane_of(L);
-    for (int i : order) {
-        int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[l] += nz_of[i];
-        lane_of[l].push_back(i);
-    }
-    std::vector<int> newpos(M), row_orig(M), lane_rows(L + 1, 0);
-    {
-        int k = 0;
-        for (int l = 0; l < L; l++) {
-            std::sort(lane_of[l].begin(), lane_of[l].end());
-            for (int i : lane_of[l]) { newpos[i] = k; row_orig[k] = rows_reached[i]; k++; }
-            lane_rows[l + 1] = k;
-        }
-    }
+    p->last_launches = 0;
+    if (M == 0) return SSS_OK;
+    if (M > 65534) return fail(SSS_EINVAL, "batched kernel supports at most 65534 reachable rows");
     std::vector<int> pos_of_orig(N, -1);
-    for (int k = 0; k < M; k++) pos_of_orig[row_orig[k]] = k;
-    std::vector<int> rows(M + 1, 0), cols;
-    std::vector<std::vector<double>> vals(G);
+    for (int k = 0; k < M; k++) pos_of_orig[rows_reached[k]] = k;
+    // pruned pattern per reachable row: (compressed col, index into sp.val)
+    struct Ent { int col; int q; };
+    std::vector<std::vector<Ent>> row_ents(M);
+    long nnz = 0;
     for (int k = 0; k < M; k++) {
-        int r = row_orig[k];
+        int r = rows_reached[k];
         for (int q = sp.row_ptr[r]; q < sp.row_ptr[r + 1]; q++) {
             int c = sp.col[q];
             if (!reach[c]) continue;
-            cols.push_back(pos_of_orig[c]);
-            for (int g = 0; g < G; g++) vals[g].push_back(sp.val[(size_t)g * sp.nnz + q]);
+            bool nz = false;
+            for (int g : active) nz |= sp.val[(size_t)g * sp.nnz + q] != 0.0;
+            if (!nz) continue;
+            row_ents[k].push_back({pos_of_orig[c], q});
+            nnz++;
         }
-        rows[k + 1] = (int)cols.size();
     }
-    const int nnz = (int)cols.size();
-    std::vector<double> hv;
-    for (int g = 0; g < G; g++) hv.insert(hv.end(), vals[g].begin(), vals[g].end());
-    std::vector<double> rw(M, 0.0);
-    if (h_rw)
-        for (int k = 0; k < M; k++) rw[k] = h_rw[row_orig[k]];
 
     // ---- norm bound -> Taylor degree and sub-steps ----
-    std::vector<double> h_prog((size_t)ntraj * nch * nseg * 5);
-    SSS_CUDA(cudaMemcpyAsync(h_prog.data(), d_prog, sizeof(double) * h_prog.size(), cudaMemcpyDeviceToHost, st));
-    SSS_CUDA(cudaStreamSynchronize(st));
-    std::vector<double> cmax(G, 0.0);
-    cmax[0] = 1.0;
-    for (int b = 0; b < ntraj; b++)
-        for (int c = 0; c < nch && c + 1 < G; c++)
-            for (int s = 0; s < nseg; s++) {
-                const double* q = &h_prog[(((size_t)b * nch + c) * nseg + s) * 5];
-                cmax[c + 1] = std::max(cmax[c + 1], std::fabs(q[1]) + std::fabs(q[2]));
-            }
     double wsum = 0.0;
     for (int e = 0; e < p->d.K; e++) {
         double s = 0.0;
@@ -384,82 +533,178 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
         wsum = std::max(wsum, s);
     }
     double beta = 0.0;
-    for (int g = 0; g < G; g++) {
-        // 1-norm of the generator restricted to reachable rows/cols
+    for (int g : active) {
         std::vector<double> colsum(M, 0.0);
         for (int k = 0; k < M; k++)
-            for (int q = rows[k]; q < rows[k + 1]; q++) colsum[cols[q]] += std::fabs(vals[g][q - 0 * rows[0]]);
-        double n1 = colsum.empty() ? 0.0 : *std::max_element(colsum.begin(), colsum.end());
-        beta += cmax[g] * n1;
+            for (const Ent& en : row_ents[k]) colsum[en.col] += std::fabs(sp.val[(size_t)g * sp.nnz + en.q]);
+        beta += cmax[g] * *std::max_element(colsum.begin(), colsum.end());
     }
     beta *= wsum * dt / F;
     int degree, substeps;
     choose_taylor(beta, p->d.taylor_degree, &degree, &substeps);
 
-    // ---- upload the pattern ----
+    // ---- lanes per trajectory ----
+    // GB300 FP64 (~2 DFMA/clk/SM, 75-cycle latency) wants several warps per
+    // SM.  Take the fewest lanes giving ~8 warps per SM, capped by the rows
+    // available to split.
+    int L = 2;
+    {
+        const long want = (long)p->num_sms * 8 * 32;
+        int cap = 2;
+        while (cap < 32 && cap * 2 <= std::max(2, M)) cap *= 2;
+        while (L < cap && (long)ntraj * L < want) L *= 2;
+    }
+    if (p->batch_lanes > 0) L = p->batch_lanes;
+    // ---- rows to lanes, balanced by entry count.  The register variant
+    // pads each row to an even length (two chains); an empty row carries
+    // zero entries so that it still closes ----
+    int epl = 0;
+    bool use_reg = false;
+    std::vector<std::vector<int>> lane_of;
+    auto assign = [&](bool pad2) {
+        auto cost = [&row_ents, pad2](int i) {
+            int n = std::max<int>(1, (int)row_ents[i].size());
+            return pad2 ? ((n + 1) & ~1) : n;
+        };
+        std::vector<int> order(M);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+        std::vector<long> load(L, 0);
+        lane_of.assign(L, {});
+        for (int i : order) {
+            int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[l] += cost(i);
+            lane_of[l].push_back(i);
+        }
+        for (auto& lo : lane_of) std::sort(lo.begin(), lo.end());
+        return std::make_pair((int)*std::max_element(load.begin(), load.end()),
+                              std::function<int(int)>(cost));
+    };
+    auto reg_try = assign(true);
+    if (reg_try.first <= 64 && p->batch_variant != 2) {
+        use_reg = true;
+        epl = 8;
+        while (epl < reg_try.first) epl *= 2;
+    }
+    auto plan_lanes = use_reg ? reg_try : assign(false);
+    const std::function<int(int)>& cost = plan_lanes.second;
+    const int E = use_reg ? epl : plan_lanes.first;
+    const int threads = p->batch_threads > 0 ? p->batch_threads : 64;
+    if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
+
+    // compressed row index = position in the lane-ordered list
+    std::vector<int> newpos(M), row_orig(M);
+    {
+        int k = 0;
+        for (int l = 0; l < L; l++)
+            for (int i : lane_of[l]) { newpos[i] = k; row_orig[k] = rows_reached[i]; k++; }
+    }
+    std::vector<double> rw(M, 0.0);
+    if (h_rw)
+        for (int k = 0; k < M; k++) rw[k] = h_rw[row_orig[k]];
     std::vector<double> toff(F), noff(p->d.Q);
     for (int r = 0; r < F; r++) toff[r] = ((double)r * dt) / F;
     for (int k = 0; k < p->d.Q; k++) noff[k] = (dt * p->nodes[k]) / F;
-    rw.insert(rw.end(), toff.begin(), toff.end());
-    rw.insert(rw.end(), noff.begin(), noff.end());
-    size_t words = hv.size() + rw.size();
-    size_t ints = rows.size() + cols.size() + lane_rows.size() + row_orig.size();
-    if (int rc = p->d_sp_val.ensure(sizeof(double) * words + sizeof(int) * ints + 64)) return rc;
-    double* dv = p->d_sp_val.as<double>();
-    int* di = reinterpret_cast<int*>(dv + words);
-    std::vector<char> blob(sizeof(double) * words + sizeof(int) * ints);
-    memcpy(blob.data(), hv.data(), sizeof(double) * hv.size());
-    memcpy(blob.data() + sizeof(double) * hv.size(), rw.data(), sizeof(double) * rw.size());
-    int* bi = reinterpret_cast<int*>(blob.data() + sizeof(double) * words);
-    memcpy(bi, rows.data(), sizeof(int) * rows.size());
-    memcpy(bi + rows.size(), cols.data(), sizeof(int) * cols.size());
-    memcpy(bi + rows.size() + cols.size(), lane_rows.data(), sizeof(int) * lane_rows.size());
-    memcpy(bi + rows.size() + cols.size() + lane_rows.size(), row_orig.data(), sizeof(int) * row_orig.size());
-    SSS_CUDA(cudaMemcpyAsync(dv, blob.data(), blob.size(), cudaMemcpyHostToDevice, st));
+
+    // generator values [g][e][l] and entry words [e][l]
+    std::vector<double> dbl((size_t)Ga * E * L, 0.0);
+    std::vector<unsigned> words((size_t)E * L, 0u);
+    std::vector<int> ints(L, 0);  // entries per lane, then row_orig
+    for (int l = 0; l < L; l++) {
+        int e = 0;
+        for (int i : lane_of[l]) {
+            const auto& ents = row_ents[i];
+            int n = cost(i);
+            for (int j = 0; j < n; j++) {
+                int col = j < (int)ents.size() ? ents[j].col : i;
+                unsigned w = (unsigned)newpos[col];
+                if (j == n - 1) w |= (unsigned)(newpos[i] + 1) << 16;
+                words[(size_t)(e + j) * L + l] = w;
+                if (j < (int)ents.size())
+                    for (int gi = 0; gi < Ga; gi++)
+                        dbl[((size_t)gi * E + e + j) * L + l] = sp.val[(size_t)active[gi] * sp.nnz + ents[j].q];
+            }
+            e += n;
+        }
+        ints[l] = e;
+    }
+    const size_t n_gv = dbl.size();
+    dbl.insert(dbl.end(), rw.begin(), rw.end());
+    dbl.insert(dbl.end(), toff.begin(), toff.end());
+    dbl.insert(dbl.end(), noff.begin(), noff.end());
+    ints.insert(ints.end(), row_orig.begin(), row_orig.end());
+    size_t bytes = sizeof(double) * dbl.size() + sizeof(unsigned) * words.size() + sizeof(int) * ints.size();
+    if (int rc = p->d_sp_val.ensure(bytes + 64)) return rc;
+    std::vector<char> blob(bytes);
+    memcpy(blob.data(), dbl.data(), sizeof(double) * dbl.size());
+    memcpy(blob.data() + sizeof(double) * dbl.size(), words.data(), sizeof(unsigned) * words.size());
+    memcpy(blob.data() + sizeof(double) * dbl.size() + sizeof(unsigned) * words.size(), ints.data(),
+           sizeof(int) * ints.size());
+    SSS_CUDA(cudaMemcpyAsync(p->d_sp_val.p, blob.data(), bytes, cudaMemcpyHostToDevice, st));
     if (int rc = p->w_queue.ensure(sizeof(int) * 4)) return rc;
     SSS_CUDA(cudaMemsetAsync(p->w_queue.p, 0, sizeof(int) * 4, st));
+    const double* dv = p->d_sp_val.as<double>();
+    const unsigned* dw = reinterpret_cast<const unsigned*>(dv + dbl.size());
+    const int* di = reinterpret_cast<const int*>(dw + words.size());
 
     BatchArgs a{};
-    a.M = M; a.G = G; a.K = p->d.K; a.Q = p->d.Q; a.F = F; a.nch = nch; a.nseg = nseg;
-    a.T_max = T_max; a.ntraj = ntraj; a.degree = degree; a.substeps = substeps; a.nnz = nnz;
+    a.M = M; a.Ga = Ga; a.K = p->d.K; a.Q = p->d.Q; a.F = F; a.nch = nch; a.nseg = nseg;
+    a.T_max = T_max; a.ntraj = ntraj; a.degree = degree; a.substeps = substeps; a.N = N;
+    a.E = E;
     a.h_sub = dt / F / substeps; a.t0 = t0; a.dt = dt;
+    for (int gi = 0; gi < Ga; gi++) a.gen_index[gi] = active[gi];
     a.W = p->d_gens.as<double>() + p->gens.size();
-    a.nodes = a.W + p->d.K * p->d.Q;
-    a.vals = dv;
-    a.rw = h_rw ? dv + hv.size() : nullptr;
-    a.toff = dv + hv.size() + M;
+    a.gv = dv;
+    a.rw = h_rw ? dv + n_gv : nullptr;
+    a.toff = dv + n_gv + M;
     a.noff = a.toff + F;
-    a.rows = di;
-    a.cols = di + rows.size();
-    a.lane_rows = di + rows.size() + cols.size();
-    a.row_orig = di + rows.size() + cols.size() + lane_rows.size();
-    a.rho0 = d_rho0; a.prog = d_prog; a.samples = d_samples; a.N = N;
+    a.ent = dw;
+    a.lane_rows = di;
+    a.row_orig = di + L;
+    a.rho0 = d_rho0; a.prog = d_prog; a.samples = d_samples;
     a.readout = d_readout; a.fin = d_final;
     a.queue = p->w_queue.as<int>();
     for (int j = 0; j <= kMaxTaylor; j++) a.inv_j[j] = j ? 1.0 / j : 0.0;
 
-    const int threads = p->batch_threads > 0 ? p->batch_threads : 128;
-    size_t shared_words = (size_t)G * nnz + M + ((M + 1 + nnz + L + 1 + 1) / 2);
-    size_t per_slot = (size_t)nnz + 4 * M + kMaxQ * kMaxG;
-    size_t smem = sizeof(double) * (shared_words + (threads / L) * per_slot);
-    if (smem > 227 * 1024)
-        return fail(SSS_EINVAL, "batched kernel needs " + std::to_string(smem) +
-                                    " bytes of shared memory per CTA (max 232448); use more lanes per trajectory");
     int rc;
-    switch (L) {
-        case 1: rc = launch_batch<1>(p, a, threads, smem, st); break;
-        case 2: rc = launch_batch<2>(p, a, threads, smem, st); break;
-        case 4: rc = launch_batch<4>(p, a, threads, smem, st); break;
-        case 8: rc = launch_batch<8>(p, a, threads, smem, st); break;
-        case 16: rc = launch_batch<16>(p, a, threads, smem, st); break;
-        default: rc = launch_batch<32>(p, a, threads, smem, st); break;
+    if (use_reg) {
+        const size_t per_slot = (3 * (size_t)M + kMaxQ * kMaxG) | 1;
+        const size_t smem = sizeof(double) * ((threads / L) * per_slot + M);
+        if (smem > 227 * 1024) return fail(SSS_EINVAL, "batched kernel: shared memory per CTA too large");
+        switch (L) {
+            case 1: rc = launch_reg<1>(p, epl, a, threads, smem, st); break;
+            case 2: rc = launch_reg<2>(p, epl, a, threads, smem, st); break;
+            case 4: rc = launch_reg<4>(p, epl, a, threads, smem, st); break;
+            case 8: rc = launch_reg<8>(p, epl, a, threads, smem, st); break;
+            case 16: rc = launch_reg<16>(p, epl, a, threads, smem, st); break;
+            default: rc = launch_reg<32>(p, epl, a, threads, smem, st); break;
+        }
+    } else {
+        const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
+        const size_t per_slot = ((size_t)E * L + 3 * M + kMaxQ * kMaxG) | 1;
+        const size_t smem = sizeof(double) * (shared_words + (threads / L) * per_slot);
+        if (smem > 227 * 1024)
+            return fail(SSS_EINVAL, "batched kernel needs " + std::to_string(smem) +
+                                        " bytes of shared memory per CTA (max 232448); use fewer "
+                                        "threads per CTA");
+        switch (L) {
+            case 1: rc = launch(p, k_batch_lanes<1>, a, threads, threads, smem, st); break;
+            case 2: rc = launch(p, k_batch_lanes<2>, a, threads, threads / 2, smem, st); break;
+            case 4: rc = launch(p, k_batch_lanes<4>, a, threads, threads / 4, smem, st); break;
+            case 8: rc = launch(p, k_batch_lanes<8>, a, threads, threads / 8, smem, st); break;
+            case 16: rc = launch(p, k_batch_lanes<16>, a, threads, threads / 16, smem, st); break;
+            default: rc = launch(p, k_batch_lanes<32>, a, threads, threads / 32, smem, st); break;
+        }
     }
     p->last_launches = rc == SSS_OK ? 1 : 0;
     p->last_batch_lanes = L;
     p->last_degree = degree;
     p->last_substeps = substeps;
     p->last_rows = M;
-    p->last_nnz = nnz;
+    p->last_nnz = (int)nnz;
+    p->last_epl = E;
+    p->last_variant = use_reg ? 1 : 2;
+    p->last_active = Ga;
     return rc;
 }
 

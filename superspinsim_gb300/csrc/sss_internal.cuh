@@ -68,7 +68,8 @@ struct sss_plan {
     int batch_lanes = 0;    // 0: chosen per run
     int batch_threads = 0;  // CTA size of the batched kernel, 0: 128
     int last_batch_lanes = 0, last_degree = 0, last_substeps = 0, last_rows = 0,
-        last_nnz = 0;
+        last_nnz = 0, last_grid = 0, last_epl = 0, last_active = 0, last_variant = 0;
+    int batch_variant = 0;  // 0: register variant when it fits, 2: shared-memory variant
     int device = 0;
     int num_sms = 0;
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // around the last batched kernel

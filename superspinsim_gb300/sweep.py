@@ -39,14 +39,14 @@ class Sweep:
     """A batched simulator for lab-frame generators (G, N, N)."""
 
     def __init__(self, generators, vectorisation_map=None, number_of_exponentials=2,
-                 number_of_fine_divisions=1, lanes=0, cta_threads=0):
+                 number_of_fine_divisions=1, lanes=0, cta_threads=0, variant=0):
         self.generators = np.ascontiguousarray(generators, dtype=np.float64)
         self.vectorisation_map = vectorisation_map
         self.N = self.generators.shape[1]
         self.F = int(number_of_fine_divisions)
         W, nodes = method(number_of_exponentials)
         self.plan = _lib.Plan(self.generators, W, nodes)
-        self.plan.set_batch_config(lanes, cta_threads)
+        self.plan.set_batch_config(lanes, cta_threads, variant)
 
     def flatten(self, rho0):
         rho0 = np.asarray(rho0)

@@ -27,8 +27,8 @@ def _excited_weights(vmap):
 
 
 @pytest.mark.parametrize("name", ["nv7_n49", "nv7_n19"])
-@pytest.mark.parametrize("lanes", [0, 1, 4, 32])
-def test_batch_odmr_against_oracle(name, lanes):
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 2), (8, 2)])
+def test_batch_odmr_against_oracle(name, lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
     c = load_case(name)
@@ -43,7 +43,7 @@ def test_batch_odmr_against_oracle(name, lanes):
     W, nodes = method(2)
     T, dt, F = 4, 1e-9, 200
     plan = _lib.Plan(c["generators"], W, nodes)
-    plan.set_batch_config(lanes=lanes)
+    plan.set_batch_config(lanes=lanes, variant=variant)
     w = _excited_weights(vm)
     ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, readout_weights=w, want_final=True)
     info = plan.batch_info()
