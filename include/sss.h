@@ -167,6 +167,25 @@ int sss_plan_batch_info(const sss_plan* plan, int* lanes, int* degree,
  * denominator of the FP64-bound kernels. */
 int sss_fp64_peak(double* tflops, void* cuda_stream);
 
+/* Allocation-free simulate for one trajectory (no counterpart in the
+ * reference, which always allocates per call).  For callers that cannot
+ * allocate device memory -- code inside another framework's memory pool, a
+ * device whose memory is already reserved, or a context where allocation is
+ * not allowed.  It runs the plain path's kernels with a fixed 4 MiB
+ * file-scope device array as scratch and allocates nothing.
+ *   desc: N <= 52, lab frame (SSS_ROTATING rejected); generators (G*N*N),
+ *   rho0 (N), programs (nch*nseg*5) and out (T*N) are device pointers;
+ *   weights (K*Q) and nodes (Q) are host pointers.
+ * Every GPU that loads the library holds the array until exit.  All calls
+ * share it, so calls that overlap on the GPU race.  The first call on a
+ * device looks up the array's address there; make it before any stream
+ * capture.  Sizes beyond the limit return SSS_EINVAL with a message. */
+int sss_simulate_noalloc(const sss_plan_desc* desc, const double* generators,
+                         const double* weights, const double* nodes,
+                         const double* rho0, int nch, int nseg,
+                         const double* programs, double t0, double dt, int T,
+                         int F, double* out, void* cuda_stream);
+
 const char* sss_last_error(void);
 void sss_plan_destroy(sss_plan* plan);
 

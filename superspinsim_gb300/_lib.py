@@ -24,7 +24,7 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
 SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
            "sss_plan_set_batch_config", "sss_plan_batch_info",
-           "sss_fp64_peak", "sss_last_error", "sss_plan_destroy"]
+           "sss_fp64_peak", "sss_simulate_noalloc", "sss_last_error", "sss_plan_destroy"]
 
 
 class SSSError(RuntimeError):

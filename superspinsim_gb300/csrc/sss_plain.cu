@@ -21,6 +21,11 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+
 #include "sss_device.cuh"
 #include "sss_internal.cuh"
 
@@ -370,3 +375,135 @@ int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
 }
 
 }  // namespace sss
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the plain path.
+//
+// Some callers cannot allocate device memory: code running inside another
+// framework's memory pool (which would fragment or be bypassed), callers
+// on a device whose memory is already fully reserved, or callers in a
+// context where allocation is forbidden (for example while a caller-managed
+// CUDA graph is being built).  sss_simulate_noalloc runs the same two
+// kernels as sss_simulate_device for one trajectory in the lab frame, but
+// instead of a plan's buffers it uses one file-scope device array as its
+// scratch: the weight/node table, the chain's running state and a chunk of
+// step propagators.  It allocates nothing on the device or the host.
+//
+// Limits: N <= 52 (the shared-memory path), lab frame only, and the
+// step-propagator chunk must hold at least one N x N matrix (always true
+// for N <= 52).  The array is 4 MiB; every GPU that loads this library
+// keeps it until the process exits.  Every call shares it and it keeps the
+// last call's contents, so calls that overlap on the GPU (on different
+// streams, or from different host threads) race and corrupt each other.
+// The first call on a device looks up the array's device address and sets
+// the kernel's shared-memory limit on that device; make that first call
+// before any stream capture.
+// ---------------------------------------------------------------------------
+
+namespace sss {
+namespace {
+
+constexpr size_t kNoallocBytes = 4u << 20;
+constexpr int kNoallocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+struct NoallocDevice {
+    double* ptr = nullptr;
+    bool ready = false;
+};
+static NoallocDevice g_noalloc_dev[kNoallocMaxDevices];
+static std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array on the current device (set up once
+// per device, with that device current).
+int noalloc_scratch(double** out) {
+    int dev = 0;
+    SSS_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoallocMaxDevices) return fail(SSS_EINVAL, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoallocDevice& d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+        e = cudaFuncSetAttribute(k_step_propagators, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(8 * (size_t)kPlainMaxN * kPlainMaxN * sizeof(double)));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+        d.ptr = static_cast<double*>(ptr);
+        d.ready = true;
+    }
+    *out = d.ptr;
+    return SSS_OK;
+}
+
+}  // namespace
+}  // namespace sss
+
+extern "C" int sss_simulate_noalloc(const sss_plan_desc* d, const double* generators,
+                                    const double* weights, const double* nodes,
+                                    const double* rho0, int nch, int nseg,
+                                    const double* programs, double t0, double dt, int T, int F,
+                                    double* out, void* stream) {
+    using namespace sss;
+    if (!d) return fail(SSS_EINVAL, "null descriptor");
+    const int N = d->N;
+    if (N <= 0 || N > kPlainMaxN)
+        return fail(SSS_EINVAL, "sss_simulate_noalloc supports 1 <= N <= 52 (got " +
+                                    std::to_string(N) + ")");
+    if (d->G <= 0 || d->G > kMaxG || d->K <= 0 || d->K > kMaxK || d->Q <= 0 || d->Q > kMaxQ)
+        return fail(SSS_EINVAL, "bad plan shape (G, K, Q)");
+    if (d->flags & SSS_ROTATING) return fail(SSS_EINVAL, "sss_simulate_noalloc is lab-frame only");
+    if (d->expm != SSS_EXPM_REFERENCE && d->expm != SSS_EXPM_TAYLOR)
+        return fail(SSS_EINVAL, "unknown exponential algorithm");
+    if (d->expm == SSS_EXPM_REFERENCE && (d->quartic_repeats < 0 || d->quartic_repeats > 500))
+        return fail(SSS_EINVAL, "quartic_repeats out of range");
+    if (T < 0 || F <= 0) return fail(SSS_EINVAL, "bad T or F");
+    if (T == 0) return SSS_OK;
+    if (!generators || !weights || !nodes || !rho0 || !programs || !out)
+        return fail(SSS_EINVAL, "null argument");
+    if (nch < 0 || nch > kMaxCh || nseg <= 0) return fail(SSS_EINVAL, "bad program shape");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(SSS_EINVAL, "dt must be positive and finite");
+
+    double* scratch = nullptr;
+    if (int rc = noalloc_scratch(&scratch)) return rc;
+    // layout: [0, 32) weights then nodes; [32, 96) chain state; then step
+    // propagators
+    const size_t NN = (size_t)N * N;
+    double* wn = scratch;
+    double* chain_state = scratch + 32;
+    double* props = scratch + 96;
+    const size_t prop_capacity = (kNoallocBytes / sizeof(double) - 96) / NN;
+    if (prop_capacity < 1) return fail(SSS_EINVAL, "scratch too small for one propagator");
+    const int chunk = (int)std::min<size_t>((size_t)T, prop_capacity);
+
+    cudaStream_t st = (cudaStream_t)stream;
+    double host_wn[32];
+    for (int i = 0; i < d->K * d->Q; i++) host_wn[i] = weights[i];
+    for (int k = 0; k < d->Q; k++) host_wn[d->K * d->Q + k] = nodes[k];
+    SSS_CUDA(cudaMemcpyAsync(wn, host_wn, sizeof(double) * (d->K * d->Q + d->Q),
+                             cudaMemcpyHostToDevice, st));
+    const size_t smem = 8 * NN * sizeof(double);
+    for (int t_begin = 0; t_begin < T; t_begin += chunk) {
+        int Tc = std::min(chunk, T - t_begin);
+        PlainArgs a{};
+        a.N = N; a.G = d->G; a.K = d->K; a.Q = d->Q; a.F = F; a.T = Tc;
+        a.nch = nch; a.nseg = nseg; a.expm = d->expm; a.R = d->quartic_repeats;
+        a.t_offset = t_begin;
+        a.residual = (d->flags & SSS_RESIDUAL) != 0;
+        a.rotating = false;
+        a.gens = generators;
+        a.W = wn;
+        a.nodes = wn + d->K * d->Q;
+        a.prog = programs;
+        a.tab = nullptr;
+        a.t0 = t0;
+        a.dt = dt;
+        a.out = props;
+        k_step_propagators<<<dim3(Tc, 1), kPlainThreads, smem, st>>>(a);
+        SSS_CUDA(cudaGetLastError());
+        k_chain<<<1, kPlainThreads, 0, st>>>(props, rho0, nullptr, nullptr, N, Tc,
+                                             a.residual ? 1 : 0, t_begin, chain_state, out);
+        SSS_CUDA(cudaGetLastError());
+    }
+    return SSS_OK;
+}
