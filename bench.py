@@ -47,6 +47,9 @@ F_RES = 2.870e9 + GAMMA*B_FIELD
 RABI = 5e6
 LASER = 10/65.9
 METRIC = "NV-7 ODMR traj-steps/s"
+# DRAM bytes (read + write) of one batched-kernel launch on this workload,
+# from ncu (profiles/batch_odmr_nv7.md)
+TRAFFIC_BYTES = 592896
 
 
 def nv7_model():
@@ -310,6 +313,19 @@ def main():
     h2d = rho0.nbytes + progs.nbytes
     d2h = B*T*8
 
+    # the plain per-trajectory drop-in (generate_simulator / simulate) on a
+    # subset of the same workload: 1 trajectory, 64 output samples
+    from superspinsim_gb300 import generate_simulator
+    plain_sim = generate_simulator(progs[0], gens, vm, number_of_exponentials=K_EXP,
+                                   number_of_fine_divisions=F)
+    plain_T = 64
+    plain_sim(rho, 0.0, 8*DT_OUT + 1e-13, DT_OUT)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain_sim(rho, 0.0, plain_T*DT_OUT + 1e-13, DT_OUT)
+    plain_s = time.perf_counter() - t
+    plain_value = plain_T*F/plain_s
+
     fl = flops_per_traj_step(info, gens.shape[0], K_EXP)
     kms = statistics.mean(kernel_ms)
     achieved = fl*B*T*F/(kms*1e-3)/1e12
@@ -331,8 +347,16 @@ def main():
             "e2e": {"value": e2e_value, "unit": "traj-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
+            "plain_dropin": {"value": plain_value, "unit": "traj-steps/s",
+                             "sample": f"generate_simulator/simulate, 1 trajectory x "
+                                       f"{plain_T*F} steps of the workload",
+                             "batched_over_plain": value/plain_value},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": achieved/peak, "traffic": None,
+                         "unit": "TFLOP/s", "frac": achieved/peak,
+                         "traffic": TRAFFIC_BYTES,
+                         "traffic_note": "dram read+write of one launch from an ncu capture "
+                                         "(profiles/batch_odmr_nv7.md); inputs are read once, "
+                                         "so it does not grow with the step count",
                          "peak_source": "measured live (sss_fp64_peak DFMA loop)",
                          "flops_per_traj_step": fl},
             "clocks": clock_info,

@@ -55,3 +55,21 @@ def test_lindbladian_properties():
 def test_unsupported_raise():
     with pytest.raises(NotImplementedError):
         generate_atoms([[{"S": 1}]], [{}], {}, use_unitary=True)
+
+
+@pytest.mark.parametrize("name", ["qubit_hyperfine", "qubit_couple_rot_e5", "qutrit_hyperfine"])
+def test_make_rotating_matches_reference(name):
+    from superspinsim_gb300.rotating import make_rotating
+    z = load_case(name)
+    g = z["generators"]
+    new, V, Vi, d, s = make_rotating(g[0], list(g[1:]))
+    # the real eigenbasis reconstructs L0 block-diagonally
+    D = Vi @ g[0] @ V
+    scale = np.abs(g[0]).max()
+    for k in range(d.shape[0]):
+        blk = D[2*k:2*k + 2, 2*k:2*k + 2]
+        assert np.allclose(blk, [[d[k, 0], d[k, 1]], [-d[k, 1], d[k, 0]]], atol=1e-9*scale) or \
+            np.allclose(blk, [[d[k, 0], -d[k, 1]], [d[k, 1], d[k, 0]]], atol=1e-9*scale)
+    # and equals the reference's frame on the machine that made the fixtures
+    assert np.abs(V - z["vectors_real"]).max() <= 1e-12
+    assert np.abs(np.array(new) - z["generators_rotating"]).max() <= 1e-9*scale

@@ -118,3 +118,32 @@ def test_empty_window_and_errors():
         generate_simulator(c["program"], c["generators"], use_cuda=False)
     with pytest.raises(TypeError):
         generate_simulator(c["program"], c["generators"], use_cayley=True)
+
+
+def _case_by_name(name):
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    for c in make_golden.cases():
+        if c["name"] == name:
+            return c, make_golden
+    raise KeyError(name)
+
+
+@pytest.mark.parametrize("name", ["qubit_couple_res_e2", "qubit_t1_mK", "qutrit_couple",
+                                  "qubit_hyperfine", "qubit_couple_rot_e5", "spin1_c1"])
+def test_simspins_front_end_matches_reference(name):
+    """The whole front end -- this package's generator builder, rotating
+    frame and simulator -- against the reference's simspins output."""
+    from superspinsim_gb300.sugar import simspins
+    c, mg = _case_by_name(name)
+    ref = load_case(name)
+    fns = [mg.channel_fn(s) for s in c["ch"]]
+    t0, tf, dt = c["t"]
+    _, d = simspins(fns, t0, tf, dt, c["spins"], c["spin_interactions"],
+                    c["group_interactions"], c["rho0"], number_of_exponentials=c["K"],
+                    number_of_fine_divisions=c["F"], number_of_quadratic_repeats=c["R"],
+                    use_rotating=c["rot"], use_residual=c["res"],
+                    use_incoherent=c["use_incoherent"])
+    assert np.abs(d - ref["density"]).max() <= 1e-12
