@@ -76,6 +76,54 @@ def workload(n_freq=N_FREQ):
     return progs, rho
 
 
+def build_workload(name, args):
+    """(generators, vmap, programs (B,4,S,5), rho (n,n), samples or None,
+    T_max, readout levels, description dict)."""
+    from superspinsim_gb300 import models, protocols
+    from superspinsim_gb300.generators import generate_atoms
+    if name == "odmr":
+        gens, vm = nv7_model()
+        progs, rho = workload(args.n_freq)
+        T = int(round(args.duration/DT_OUT))
+        desc = {"workload": "NV-7 ODMR sweep, 1024 frequencies x 2 us at 5 ps "
+                            "(400k CF4:2 steps each), readout every 1 ns",
+                "n_freq": progs.shape[0], "n_levels": 7, "liouvillian": "49x49"}
+        return gens, vm, progs, rho, None, T, [3, 4, 5], desc
+    if name == "ramsey":
+        gens, vm = nv7_model()
+        rng = np.random.default_rng(20260103)
+        B = args.n_traj or 4096
+        rabi = rng.uniform(2e6, 10e6, B)
+        det = rng.uniform(-5e6, 5e6, B)
+        tau = rng.uniform(0, 5e-6, B)
+        progs, dur = protocols.ramsey(rabi, det, tau, F_RES, LASER)
+        samples = np.ceil(dur/DT_OUT).astype(np.int32)
+        rho = np.zeros((7, 7), complex)
+        rho[1, 1] = 1.0
+        desc = {"workload": f"NV-7 Ramsey, {B} seeded trajectories (Rabi 2-10 MHz, detuning "
+                            "+-5 MHz, tau 0-5 us; laser 1 us, pi/2, tau, pi/2, laser 0.5 us) "
+                            "at 5 ps, uneven lengths",
+                "n_traj": B, "n_levels": 7, "liouvillian": "49x49",
+                "traj_steps_total": int(samples.sum())*F}
+        return gens, vm, progs, rho, samples, int(samples.max()), [3, 4, 5], desc
+    if name == "nv21":
+        spins, inter, groups = models.nv_21(np.array([0.0, 0.0, 0.05]),
+                                            params=models.nv21_params())
+        g, vm = generate_atoms(spins, inter, groups, use_incoherent=False)
+        gens = np.array([g["generators"][k] for k in ("L0", "Gx", "Gy", "Gz", "Gr")])
+        B = args.n_traj or 256
+        f_res = 2.870e9 + GAMMA*0.05
+        progs = protocols.odmr(f_res + np.linspace(-30e6, 30e6, B), RABI, LASER)
+        rho = np.zeros((21, 21), complex)
+        for k in range(3, 6):
+            rho[k, k] = 1/3
+        T = int(round(args.duration/DT_OUT)) if args.duration != DURATION else 1000
+        desc = {"workload": f"NV-21 (NV + 14N) ODMR sweep, {B} frequencies x {T} ns at 5 ps",
+                "n_freq": B, "n_levels": 21, "liouvillian": "441x441"}
+        return gens, vm, progs, rho, None, T, list(range(9, 18)), desc
+    raise ValueError(name)
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples taken while the timed region runs."""
 
@@ -235,6 +283,8 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="odmr", choices=["odmr", "ramsey", "nv21"])
+    ap.add_argument("--n-traj", type=int, default=0)
     args = ap.parse_args()
     rank, world = dist_setup()
     if args.impl == "reference":
@@ -247,13 +297,12 @@ def main():
     from superspinsim_gb300.sweep import Sweep, population_weights, trapezoid
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    gens, vm = nv7_model()
+    gens, vm, progs, rho, samples, T, levels, wdesc = build_workload(args.workload, args)
     N = vm.shape[0]
-    progs, rho = workload(args.n_freq)
     B = progs.shape[0]
-    T = int(round(args.duration/DT_OUT))
+    units_per_step = int(samples.sum())*F if samples is not None else B*T*F
     rho0 = np.repeat(flatten_density(rho, N, vm)[None], B, axis=0)
-    w = population_weights(vm, [3, 4, 5])
+    w = population_weights(vm, levels)
     sweep = Sweep(gens, vm, number_of_exponentials=K_EXP, number_of_fine_divisions=F,
                   lanes=args.lanes, cta_threads=args.threads, variant=args.variant)
     plan = sweep.plan
@@ -261,12 +310,15 @@ def main():
     stream = torch.cuda.Stream()
     d_rho0 = torch.from_numpy(rho0).cuda()
     d_prog = torch.from_numpy(progs).cuda()
+    d_smp = torch.from_numpy(samples).cuda() if samples is not None else None
     d_ro = torch.empty((B, T), dtype=torch.float64, device="cuda")
     flush = torch.empty(256*1024*1024//4, dtype=torch.float32, device="cuda")  # > L2
 
     def step():
         plan.batch_device(d_rho0.data_ptr(), B, d_prog.data_ptr(), 4, progs.shape[2], 0.0,
-                          DT_OUT, T, F, readout_weights=w, readout_ptr=d_ro.data_ptr(),
+                          DT_OUT, T, F,
+                          samples_ptr=d_smp.data_ptr() if d_smp is not None else None,
+                          readout_weights=w, readout_ptr=d_ro.data_ptr(),
                           stream=stream.cuda_stream)
 
     with torch.cuda.stream(stream):
@@ -293,7 +345,7 @@ def main():
     info = plan.batch_info()
     launches = plan.last_launches()*args.steps
     total_ms = max_over_ranks(sum(times), world)
-    units = B*T*F*world*args.steps
+    units = units_per_step*world*args.steps
     value = units/(total_ms/1e3)
 
     # e2e: public API, host buffers in and out, every step
@@ -302,43 +354,43 @@ def main():
         torch.cuda.synchronize()
         barrier(world)
         t = time.perf_counter()
-        out = sweep.run(np.repeat(rho[None], B, axis=0), progs, 0.0, args.duration + 1e-13,
-                        DT_OUT, readout_weights=w)
+        out = sweep.run(np.repeat(rho[None], B, axis=0), progs, 0.0, T*DT_OUT + 1e-13,
+                        DT_OUT, samples=samples, readout_weights=w)
         fluor = 65.9e6*trapezoid(out["readout"], DT_OUT)
         el = time.perf_counter() - t
         if i >= 1:
             e2e_times.append(el)
     e2e_s = max_over_ranks(sum(e2e_times), world)
-    e2e_value = B*T*F*world*args.steps/e2e_s
-    h2d = rho0.nbytes + progs.nbytes
+    e2e_value = units_per_step*world*args.steps/e2e_s
+    h2d = rho0.nbytes + progs.nbytes + (samples.nbytes if samples is not None else 0)
     d2h = B*T*8
 
     # the plain per-trajectory drop-in (generate_simulator / simulate) on a
     # subset of the same workload: 1 trajectory, 64 output samples
     from superspinsim_gb300 import generate_simulator
-    plain_sim = generate_simulator(progs[0], gens, vm, number_of_exponentials=K_EXP,
-                                   number_of_fine_divisions=F)
-    plain_T = 64
-    plain_sim(rho, 0.0, 8*DT_OUT + 1e-13, DT_OUT)
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    plain_sim(rho, 0.0, plain_T*DT_OUT + 1e-13, DT_OUT)
-    plain_s = time.perf_counter() - t
-    plain_value = plain_T*F/plain_s
+    plain_value = None
+    if N <= 52:
+        plain_sim = generate_simulator(progs[0], gens, vm, number_of_exponentials=K_EXP,
+                                       number_of_fine_divisions=F)
+        plain_T = 64
+        plain_sim(rho, 0.0, 8*DT_OUT + 1e-13, DT_OUT)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        plain_sim(rho, 0.0, plain_T*DT_OUT + 1e-13, DT_OUT)
+        plain_s = time.perf_counter() - t
+        plain_value = plain_T*F/plain_s
 
     fl = flops_per_traj_step(info, gens.shape[0], K_EXP)
     kms = statistics.mean(kernel_ms)
-    achieved = fl*B*T*F/(kms*1e-3)/1e12
+    achieved = fl*units_per_step/(kms*1e-3)/1e12
     peak = _lib.fp64_peak_tflops()
     line = {"metric": METRIC, "value": value, "unit": "traj-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms/args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "NV-7 ODMR sweep, 1024 frequencies x 2 us at 5 ps "
-                                   "(400k CF4:2 steps each), readout every 1 ns",
-                       "n_freq": B, "n_levels": 7, "liouvillian": "49x49", "method": "CF4:2",
+            "config": {**wdesc, "method": "CF4:2",
                        "dt_s": DT_OUT/F, "samples": T, "fine_divisions": F,
-                       "traj_steps_per_step": B*T*F,
+                       "traj_steps_per_step": units_per_step,
                        "l2": "flushed between timed steps (256 MiB write)",
                        "kernel": {"lanes": info["lanes"], "taylor_degree": info["degree"],
                                   "substeps": info["substeps"], "rows": info["rows"],
@@ -347,13 +399,14 @@ def main():
             "e2e": {"value": e2e_value, "unit": "traj-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "plain_dropin": {"value": plain_value, "unit": "traj-steps/s",
-                             "sample": f"generate_simulator/simulate, 1 trajectory x "
-                                       f"{plain_T*F} steps of the workload",
-                             "batched_over_plain": value/plain_value},
+            "plain_dropin": None if plain_value is None else {
+                "value": plain_value, "unit": "traj-steps/s",
+                "sample": f"generate_simulator/simulate, 1 trajectory x "
+                          f"{plain_T*F} steps of the workload",
+                "batched_over_plain": value/plain_value},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved/peak,
-                         "traffic": TRAFFIC_BYTES,
+                         "traffic": TRAFFIC_BYTES if args.workload == "odmr" else None,
                          "traffic_note": "dram read+write of one launch from an ncu capture "
                                          "(profiles/batch_odmr_nv7.md); inputs are read once, "
                                          "so it does not grow with the step count",
@@ -361,7 +414,10 @@ def main():
                          "flops_per_traj_step": fl},
             "clocks": clock_info,
             "fluorescence_check": float(np.mean(fluor))}
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if args.workload != "odmr":
+        line["metric"] = {"ramsey": "NV-7 Ramsey (uneven) traj-steps/s",
+                          "nv21": "NV-21 ODMR traj-steps/s"}[args.workload]
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "odmr":
         cb = cpu_baseline()
         cb.pop("seconds", None)
         line["cpu_baseline"] = cb

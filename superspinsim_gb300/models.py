@@ -69,3 +69,55 @@ def odmr_params():
     room = types.SimpleNamespace(ground=ground, excited=excited, optical=optical, isc=isc)
     P.nv = types.SimpleNamespace(room=room)
     return P
+
+
+def nv_21(quiescent_magnetic_field=None, params=None):
+    """The 21-level NV with its 14N nucleus (spin 1) in every orbital
+    manifold: the description the reference's legacy ``generate_21``
+    builds (superspinsim/generate_generators.py:2944-3028), returned in the
+    ``nv_7`` format for ``generate_atoms`` / ``simspins``."""
+    B0 = np.zeros(3) if quiescent_magnetic_field is None else np.asarray(
+        quiescent_magnetic_field, dtype=float)
+    P = s3p if params is None else params
+    g, e = P.nv.room.ground, P.nv.room.excited
+    T = P.standards.lab.ntp.temperature
+    ground = {"S": 1, "g": g.g_longitudinal, "g_perp": g.g_transverse,
+              "D": math.tau*g.zfs_longitudinal, "TS1": g.thermalisation_time,
+              "TS2": g.dephasing_time,
+              "I": 1, "gN": g.g_N_14N_longitudinal,
+              "P": math.tau*g.nuclear_quadrupole_14N_longitudinal,
+              "TI1": g.thermalisation_time_14N, "TI2": g.dephasing_time_14N,
+              "A": math.tau*g.hyperfine_14N_longitudinal,
+              "A_perp": math.tau*g.hyperfine_14N_transverse,
+              "B0": B0, "T": T}
+    excited = {"S": 1, "g": e.g_longitudinal, "D": math.tau*e.zfs_longitudinal,
+               "TS1": e.thermalisation_time, "TS2": e.dephasing_time,
+               "I": 1, "gN": e.g_N_14N_longitudinal,
+               "P": math.tau*e.nuclear_quadrupole_14N_longitudinal,
+               "TI1": e.thermalisation_time_14N, "TI2": e.dephasing_time_14N,
+               "A": math.tau*e.hyperfine_14N_longitudinal,
+               "A_perp": math.tau*e.hyperfine_14N_transverse,
+               "B0": B0, "T": T}
+    singlet = {"S": 0, "I": 1, "gN": g.g_N_14N_longitudinal,
+               "P": math.tau*g.nuclear_quadrupole_14N_longitudinal,
+               "TI1": g.thermalisation_time_14N, "TI2": g.dephasing_time_14N,
+               "B0": B0, "T": T}
+    _, _, groups = nv_7(B0, params)
+    return [[ground], [excited], [singlet]], [{}, {}, {}], groups
+
+
+def nv21_params():
+    """The dense 21-level workload's parameters: the 7-level ODMR rates
+    (``odmr_params``) with the ground-state 14N hyperfine A_par = -2.16 MHz,
+    A_perp = -2.70 MHz and quadrupole P = -4.95 MHz."""
+    P = odmr_params()
+
+    class ground(P.nv.room.ground):
+        hyperfine_14N_longitudinal = -2.16e6
+        hyperfine_14N_transverse = -2.70e6
+        nuclear_quadrupole_14N_longitudinal = -4.95e6
+
+    room = types.SimpleNamespace(ground=ground, excited=P.nv.room.excited,
+                                 optical=P.nv.room.optical, isc=P.nv.room.isc)
+    P.nv = types.SimpleNamespace(room=room)
+    return P

@@ -40,12 +40,26 @@ class nv:
             zfs_longitudinal = 2872000000.0
             g_longitudinal = 2.000536581621305
             g_transverse = 2.0031
+            # 14N nuclear spin in the ground state
+            thermalisation_time_14N = 10.0
+            dephasing_time_14N = 9.999999999999999e-06
+            nuclear_quadrupole_14N_longitudinal = -4945000.0
+            hyperfine_14N_longitudinal = -2162000.0
+            hyperfine_14N_transverse = -2620000.0
+            g_N_14N_longitudinal = 0.40366839834155777
 
         class excited:
             thermalisation_time = 0.001
             dephasing_time = 1e-08
             zfs_longitudinal = 1423000000.0
             g_longitudinal = 2.0019655363224635
+            # 14N nuclear spin in the excited state
+            thermalisation_time_14N = 0.1
+            dephasing_time_14N = 0.001
+            nuclear_quadrupole_14N_longitudinal = -4945000.0
+            hyperfine_14N_longitudinal = -40000000.0
+            hyperfine_14N_transverse = -23000000.0
+            g_N_14N_longitudinal = 0.4040619651907696
 
         class isc:
             s_gets_pm = 60400000.0

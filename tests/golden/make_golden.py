@@ -310,6 +310,50 @@ def nv7_params(params):
     return copy.copy(P)
 
 
+def nv21_case():
+    """The 21-level NV (14N spin 1 in every orbital manifold, as in the
+    reference's legacy generate_21, generate_generators.py:2944-3028) at
+    50 mT with the 7-level ODMR rates and the ground-state 14N constants
+    A_par = -2.16 MHz, A_perp = -2.70 MHz, P = -4.95 MHz.  Generators only:
+    the reference's simulate is pure Python under the shim and too slow at
+    N = 441."""
+    from superspinsim import params
+    P = nv7_params(params)
+    g, e = P.nv.room.ground, P.nv.room.excited
+    B0 = np.array([0, 0, 0.05])
+    T = params.standards.lab.ntp.temperature
+    ground = {"S": 1, "g": g.g_longitudinal, "g_perp": g.g_transverse,
+              "D": math.tau*g.zfs_longitudinal, "TS1": g.thermalisation_time,
+              "TS2": g.dephasing_time, "I": 1, "gN": g.g_N_14N_longitudinal,
+              "P": math.tau*(-4.95e6), "TI1": g.thermalisation_time_14N,
+              "TI2": g.dephasing_time_14N, "A": math.tau*(-2.16e6),
+              "A_perp": math.tau*(-2.70e6), "B0": B0, "T": T}
+    excited = {"S": 1, "g": e.g_longitudinal, "D": math.tau*e.zfs_longitudinal,
+               "TS1": e.thermalisation_time, "TS2": e.dephasing_time, "I": 1,
+               "gN": e.g_N_14N_longitudinal,
+               "P": math.tau*e.nuclear_quadrupole_14N_longitudinal,
+               "TI1": e.thermalisation_time_14N, "TI2": e.dephasing_time_14N,
+               "A": math.tau*e.hyperfine_14N_longitudinal,
+               "A_perp": math.tau*e.hyperfine_14N_transverse, "B0": B0, "T": T}
+    singlet = {"S": 0, "I": 1, "gN": g.g_N_14N_longitudinal,
+               "P": math.tau*(-4.95e6), "TI1": g.thermalisation_time_14N,
+               "TI2": g.dephasing_time_14N, "B0": B0, "T": T}
+    from superspinsim import models
+    _, _, groups = models.nv_7(B0, params=P)
+    return [[ground], [excited], [singlet]], [{}, {}, {}], groups
+
+
+def save_nv21():
+    from superspinsim.generate_generators import generate_atoms
+    spins, inter, groups = nv21_case()
+    t = _time.time()
+    g, vm = generate_atoms(spins, inter, groups, False, True, False)
+    gens = np.array([g["generators"][k] for k in ["L0", "Gx", "Gy", "Gz", "Gr"]])
+    np.savez_compressed(os.path.join(HERE, "nv21_n441.npz"), generators=gens,
+                        vectorisation_map=vm)
+    print(f"nv21_n441: N={gens.shape[1]} {_time.time() - t:.1f} s", flush=True)
+
+
 def build_generators(c):
     from superspinsim.generate_generators import generate_atoms, \
         make_rotating
@@ -398,6 +442,8 @@ def main():
         if only and c["name"] not in only:
             continue
         save_case(c)
+    if not only or "nv21_n441" in only:
+        save_nv21()
 
 
 if __name__ == "__main__":

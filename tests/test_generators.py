@@ -69,3 +69,14 @@ def test_make_rotating_matches_reference(name):
     # and equals the reference's frame on the machine that made the fixtures
     assert np.abs(V - z["vectors_real"]).max() <= 1e-12
     assert np.abs(np.array(new) - z["generators_rotating"]).max() <= 1e-9*scale
+
+
+def test_nv21_model_matches_reference():
+    """21-level NV with 14N (441 x 441 Liouvillian)."""
+    z = load_case("nv21_n441")
+    spins, inter, groups = models.nv_21(np.array([0, 0, 0.05]), params=models.nv21_params())
+    g, vm = generate_atoms(spins, inter, groups, use_incoherent=False)
+    assert np.array_equal(vm, z["vectorisation_map"])
+    for i, k in enumerate(LABELS):
+        ref = z["generators"][i]
+        assert np.abs(g["generators"][k] - ref).max() <= 1e-15*np.abs(ref).max()

@@ -100,3 +100,63 @@ def test_batch_empty_and_zero_state():
     ro, fin = plan.batch(np.zeros((0, N)), progs[:0], 0.0, 1e-9, 3, 10,
                          readout_weights=np.ones(N), want_final=True)
     assert ro.shape == (0, 3)
+
+
+def test_batch_ramsey_uneven_against_oracle():
+    """Uneven Ramsey protocol (laser init, pi/2 - tau - pi/2, laser readout)
+    with per-trajectory lengths, against the oracle trajectory by trajectory."""
+    from superspinsim_gb300 import _lib, protocols
+    from superspinsim_gb300.quadratures import method
+    c = load_case("nv7_n19")
+    vm = c["vectorisation_map"]
+    N = vm.shape[0]
+    rng = np.random.default_rng(11)
+    B = 9
+    f_res = 2.870e9 + 28.025e9*5e-3
+    rabi = rng.uniform(20e6, 60e6, B)
+    det = rng.uniform(-5e6, 5e6, B)
+    tau = rng.uniform(0, 30e-9, B)
+    progs, dur = protocols.ramsey(rabi, det, tau, f_res, 10/65.9, t_init=20e-9, t_read=10e-9)
+    dt, F = 1e-9, 40
+    samples = np.ceil(dur/dt).astype(np.int32)
+    T = int(samples.max())
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1
+    rho0 = np.stack([oracle.flatten(rho, vm, N)]*B)
+    W, nodes = method(2)
+    plan = _lib.Plan(c["generators"], W, nodes)
+    w = _excited_weights(vm)
+    ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, samples=samples, readout_weights=w,
+                         want_final=True)
+    for b in range(B):
+        n = int(samples[b])
+        _, ref = oracle.simulate(c["generators"], rho, 0.0, n*dt + 1e-13, dt, progs[b], K=2,
+                                 W=W, nodes=nodes, F=F, vectorisation_map=vm, mode="vector",
+                                 degree=16, flat_out=True)
+        assert np.abs(ro[b, :n] - ref @ w).max() <= 1e-12
+        assert np.abs(fin[b] - ref[-1]).max() <= 1e-12
+
+
+def test_batch_nv21_against_oracle():
+    """21-level NV with 14N (441 x 441), 4 ODMR trajectories."""
+    from superspinsim_gb300 import _lib, protocols
+    from superspinsim_gb300.quadratures import method
+    c = load_case("nv21_n441")
+    gens, vm = c["generators"], c["vectorisation_map"]
+    N = vm.shape[0]
+    f_res = 2.870e9 + 28.025e9*0.05
+    progs = protocols.odmr(f_res + np.array([-3e6, -1e6, 1e6, 3e6]), 5e6, 10/65.9)
+    rho = np.zeros((21, 21), complex)
+    for k in range(3, 6):
+        rho[k, k] = 1/3    # ms = 0 with the nitrogen spin mixed
+    rho0 = np.stack([oracle.flatten(rho, vm, N)]*4)
+    W, nodes = method(2)
+    T, dt, F = 2, 1e-9, 50
+    plan = _lib.Plan(gens, W, nodes)
+    ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, want_final=True)
+    info = plan.batch_info()
+    assert info["rows"] < N
+    _, ref = oracle.simulate(gens, np.stack([rho]*4), 0.0, T*dt + 1e-13, dt, progs, K=2, W=W,
+                             nodes=nodes, F=F, vectorisation_map=vm, mode="vector", degree=16,
+                             flat_out=True)
+    assert np.abs(fin - ref[:, -1]).max() <= 1e-12
