@@ -140,6 +140,24 @@ int sss_batch_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                   const double* readout_weights, double* readout,
                   double* final_state, int host, void* cuda_stream);
 
+/* Adjoint gradients (no reference counterpart: the reference computes no
+ * derivatives).  For each trajectory, the objective
+ *   J = sum_t time_weights[t] * dot(readout_weights, state after sample t)
+ * (for example integrated fluorescence: excited populations times the
+ * decay rate, trapezoid weights over the readout window) and its gradient
+ * with respect to the amplitude and phase of every segment of channel 0
+ * (the x field):  grad[(b*nseg + s)*2 + 0] = dJ/d amplitude_s,
+ * grad[(b*nseg + s)*2 + 1] = dJ/d phase_s.  Forward pass with
+ * sqrt(T*F)-step checkpoints, then a backward sweep that recomputes each
+ * interval; the exponential's derivative is exact for the truncated series
+ * the forward pass uses.  Lab frame.  readout_weights (N) and time_weights
+ * (T) are host arrays; the rest follow `host` as in sss_batch_run. */
+int sss_adjoint_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
+                    int nseg, const double* programs, double t0, double dt,
+                    int T, int F, const double* readout_weights,
+                    const double* time_weights, double* J, double* grad,
+                    int host, void* cuda_stream);
+
 /* Kernel launches issued by the last sss_simulate / sss_batch_run call on
  * this plan (for launch accounting). */
 int sss_plan_last_launches(const sss_plan* plan);

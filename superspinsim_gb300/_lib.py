@@ -24,7 +24,8 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
 SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
            "sss_plan_set_batch_config", "sss_plan_batch_info",
-           "sss_fp64_peak", "sss_simulate_noalloc", "sss_last_error", "sss_plan_destroy"]
+           "sss_fp64_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_last_error",
+           "sss_plan_destroy"]
 
 
 class SSSError(RuntimeError):
@@ -74,6 +75,8 @@ def load(build_if_missing=True):
         L.sss_plan_set_batch_config.argtypes = [vp, i, i, i]
         L.sss_plan_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, dp]
         L.sss_fp64_peak.argtypes = [dp, vp]
+        L.sss_adjoint_run.argtypes = [vp, i, vp, i, i, vp, d, d, i, i, dp, dp, vp, vp, i, vp]
+        L.sss_adjoint_run.restype = i
         L.sss_fp64_peak.restype = i
         L.sss_last_error.restype = ctypes.c_char_p
         L.sss_plan_destroy.argtypes = [vp]
@@ -200,6 +203,24 @@ class Plan:
         check(load().sss_batch_run(self._h, B, rho0_ptr, nch, nseg, programs_ptr,
                                    samples_ptr, float(t0), float(dt), int(T_max),
                                    int(F), dptr(rw), readout_ptr, final_ptr, 0, stream))
+
+    def adjoint(self, rho0, programs, t0, dt, T, F, readout_weights, time_weights, stream=None):
+        """Host-buffer adjoint run.  Returns (J (B,), grad (B, nseg, 2))."""
+        rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
+        programs = np.ascontiguousarray(programs, dtype=np.float64)
+        B = rho0.shape[0]
+        nch, nseg = programs.shape[1], programs.shape[2]
+        J = np.empty(B)
+        grad = np.empty((B, nseg, 2))
+        rw = np.ascontiguousarray(readout_weights, dtype=np.float64)
+        tw = np.ascontiguousarray(time_weights, dtype=np.float64)
+        assert tw.size == T
+        check(load().sss_adjoint_run(
+            self._h, B, rho0.ctypes.data_as(ctypes.c_void_p), nch, nseg,
+            programs.ctypes.data_as(ctypes.c_void_p), float(t0), float(dt), int(T), int(F),
+            dptr(rw), dptr(tw), J.ctypes.data_as(ctypes.c_void_p),
+            grad.ctypes.data_as(ctypes.c_void_p), 1, stream))
+        return J, grad
 
     def set_batch_config(self, lanes=0, cta_threads=0, variant=0):
         check(load().sss_plan_set_batch_config(self._h, int(lanes), int(cta_threads),

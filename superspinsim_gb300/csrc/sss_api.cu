@@ -306,6 +306,50 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
     return SSS_OK;
 }
 
+int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                    const double* programs, double t0, double dt, int T, int F,
+                    const double* readout_weights, const double* time_weights, double* J,
+                    double* grad, int host, void* stream) {
+    if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, T, F,
+                           (const void*)J))
+        return rc;
+    if (!programs || !readout_weights || !time_weights || !grad)
+        return fail(SSS_EINVAL, "the adjoint needs programs, readout and time weights, and grad");
+    if (p->rotating) return fail(SSS_EINVAL, "the adjoint supports the lab frame only");
+    p->last_launches = 0;
+    if (ntraj == 0 || T == 0) return SSS_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int N = p->d.N;
+    const double *d_rho0 = rho0, *d_prog = programs;
+    double *d_J = J, *d_grad = grad;
+    size_t nprog = (size_t)ntraj * nch * nseg * 5;
+    if (host) {
+        for (size_t i = 0; i < nprog; i++)
+            if (std::isnan(programs[i])) return fail(SSS_ENONFINITE, "program contains NaN");
+        if (int rc = p->w_in.ensure(sizeof(double) * ((size_t)ntraj * N + nprog))) return rc;
+        if (int rc = p->w_out.ensure(sizeof(double) * ((size_t)ntraj + (size_t)ntraj * nseg * 2)))
+            return rc;
+        double* base = p->w_in.as<double>();
+        SSS_CUDA(cudaMemcpyAsync(base, rho0, sizeof(double) * ntraj * N, cudaMemcpyHostToDevice, st));
+        SSS_CUDA(cudaMemcpyAsync(base + (size_t)ntraj * N, programs, sizeof(double) * nprog,
+                                 cudaMemcpyHostToDevice, st));
+        d_rho0 = base;
+        d_prog = base + (size_t)ntraj * N;
+        d_J = p->w_out.as<double>();
+        d_grad = d_J + ntraj;
+    }
+    if (int rc = adjoint_run(p, ntraj, d_rho0, nch, nseg, d_prog, t0, dt, T, F, readout_weights,
+                             time_weights, d_J, d_grad, st))
+        return rc;
+    if (host) {
+        SSS_CUDA(cudaMemcpyAsync(J, d_J, sizeof(double) * ntraj, cudaMemcpyDeviceToHost, st));
+        SSS_CUDA(cudaMemcpyAsync(grad, d_grad, sizeof(double) * (size_t)ntraj * nseg * 2,
+                                 cudaMemcpyDeviceToHost, st));
+        SSS_CUDA(cudaStreamSynchronize(st));
+    }
+    return SSS_OK;
+}
+
 int sss_plan_last_launches(const sss_plan* p) { return p ? p->last_launches : 0; }
 
 // FP64 FMA throughput probe: every thread runs 8 independent DFMA chains.

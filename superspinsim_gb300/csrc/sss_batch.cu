@@ -449,11 +449,11 @@ static void choose_taylor(double beta, int forced_degree, int* degree, int* subs
     *substeps = best_m;
 }
 
-int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,
-              const int* d_samples, const int* h_samples, double t0, double dt, int T_max, int F,
-              const double* h_rw, double* d_readout, double* d_final, cudaStream_t st) {
-    (void)h_samples;
+int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+                 const double* d_prog, double dt, int F, const std::vector<int>& force_active,
+                 bool allow_register, BatchLayout* out, cudaStream_t st) {
     const int N = p->d.N, G = p->d.G;
+    BatchLayout& Ly = *out;
     const SparseGenerators& sp = p->sparse;
     std::vector<double> h_rho0((size_t)ntraj * N), h_prog((size_t)ntraj * nch * nseg * 5);
     SSS_CUDA(cudaMemcpyAsync(h_rho0.data(), d_rho0, sizeof(double) * h_rho0.size(),
@@ -475,7 +475,8 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     for (int g = 0; g < G; g++) {
         bool nonzero_gen = false;
         for (int q = 0; q < sp.nnz; q++) nonzero_gen |= sp.val[(size_t)g * sp.nnz + q] != 0.0;
-        if (cmax[g] > 0.0 && nonzero_gen) active.push_back(g);
+        bool forced = std::find(force_active.begin(), force_active.end(), g) != force_active.end();
+        if ((cmax[g] > 0.0 || forced) && nonzero_gen) active.push_back(g);
     }
     const int Ga = (int)active.size();
     // ---- reachable rows from the initial states' support ----
@@ -501,16 +502,16 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     for (int i = 0; i < N; i++)
         if (reach[i]) rows_reached.push_back(i);
     const int M = (int)rows_reached.size();
-    if (d_readout) SSS_CUDA(cudaMemsetAsync(d_readout, 0, sizeof(double) * (size_t)ntraj * T_max, st));
-    if (d_final) SSS_CUDA(cudaMemsetAsync(d_final, 0, sizeof(double) * (size_t)ntraj * N, st));
-    p->last_launches = 0;
+    Ly.M = M;
+    Ly.Ga = Ga;
+    Ly.active = active;
     if (M == 0) return SSS_OK;
     if (M > 65534) return fail(SSS_EINVAL, "batched kernel supports at most 65534 reachable rows");
     std::vector<int> pos_of_orig(N, -1);
     for (int k = 0; k < M; k++) pos_of_orig[rows_reached[k]] = k;
     // pruned pattern per reachable row: (compressed col, index into sp.val)
-    struct Ent { int col; int q; };
-    std::vector<std::vector<Ent>> row_ents(M);
+    std::vector<std::vector<BatchLayout::Ent>>& row_ents = Ly.row_ents;
+    row_ents.assign(M, {});
     long nnz = 0;
     for (int k = 0; k < M; k++) {
         int r = rows_reached[k];
@@ -536,7 +537,7 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     for (int g : active) {
         std::vector<double> colsum(M, 0.0);
         for (int k = 0; k < M; k++)
-            for (const Ent& en : row_ents[k]) colsum[en.col] += std::fabs(sp.val[(size_t)g * sp.nnz + en.q]);
+            for (const BatchLayout::Ent& en : row_ents[k]) colsum[en.col] += std::fabs(sp.val[(size_t)g * sp.nnz + en.q]);
         beta += cmax[g] * *std::max_element(colsum.begin(), colsum.end());
     }
     beta *= wsum * dt / F;
@@ -581,7 +582,7 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
                               std::function<int(int)>(cost));
     };
     auto reg_try = assign(true);
-    if (reg_try.first <= 64 && p->batch_variant != 2) {
+    if (allow_register && reg_try.first <= 64 && p->batch_variant != 2) {
         use_reg = true;
         epl = 8;
         while (epl < reg_try.first) epl *= 2;
@@ -593,23 +594,20 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
 
     // compressed row index = position in the lane-ordered list
-    std::vector<int> newpos(M), row_orig(M);
+    std::vector<int>& newpos = Ly.newpos;
+    std::vector<int>& row_orig = Ly.row_orig;
+    newpos.assign(M, 0);
+    row_orig.assign(M, 0);
     {
         int k = 0;
         for (int l = 0; l < L; l++)
             for (int i : lane_of[l]) { newpos[i] = k; row_orig[k] = rows_reached[i]; k++; }
     }
-    std::vector<double> rw(M, 0.0);
-    if (h_rw)
-        for (int k = 0; k < M; k++) rw[k] = h_rw[row_orig[k]];
-    std::vector<double> toff(F), noff(p->d.Q);
-    for (int r = 0; r < F; r++) toff[r] = ((double)r * dt) / F;
-    for (int k = 0; k < p->d.Q; k++) noff[k] = (dt * p->nodes[k]) / F;
-
     // generator values [g][e][l] and entry words [e][l]
-    std::vector<double> dbl((size_t)Ga * E * L, 0.0);
-    std::vector<unsigned> words((size_t)E * L, 0u);
-    std::vector<int> ints(L, 0);  // entries per lane, then row_orig
+    Ly.gv.assign((size_t)Ga * E * L, 0.0);
+    Ly.words.assign((size_t)E * L, 0u);
+    Ly.cnt.assign(L, 0);
+    Ly.entry_q.assign((size_t)E * L, -1);
     for (int l = 0; l < L; l++) {
         int e = 0;
         for (int i : lane_of[l]) {
@@ -619,15 +617,56 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
                 int col = j < (int)ents.size() ? ents[j].col : i;
                 unsigned w = (unsigned)newpos[col];
                 if (j == n - 1) w |= (unsigned)(newpos[i] + 1) << 16;
-                words[(size_t)(e + j) * L + l] = w;
-                if (j < (int)ents.size())
+                Ly.words[(size_t)(e + j) * L + l] = w;
+                if (j < (int)ents.size()) {
+                    Ly.entry_q[(size_t)(e + j) * L + l] = ents[j].q;
                     for (int gi = 0; gi < Ga; gi++)
-                        dbl[((size_t)gi * E + e + j) * L + l] = sp.val[(size_t)active[gi] * sp.nnz + ents[j].q];
+                        Ly.gv[((size_t)gi * E + e + j) * L + l] = sp.val[(size_t)active[gi] * sp.nnz + ents[j].q];
+                }
             }
             e += n;
         }
-        ints[l] = e;
+        Ly.cnt[l] = e;
     }
+    Ly.L = L;
+    Ly.E = E;
+    Ly.use_reg = use_reg;
+    Ly.epl = epl;
+    Ly.nnz = nnz;
+    Ly.degree = degree;
+    Ly.substeps = substeps;
+    Ly.threads = threads;
+    Ly.lane_of = lane_of;
+    return SSS_OK;
+}
+
+int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,
+              const int* d_samples, const int* h_samples, double t0, double dt, int T_max, int F,
+              const double* h_rw, double* d_readout, double* d_final, cudaStream_t st) {
+    (void)h_samples;
+    const int N = p->d.N;
+    if (d_readout) SSS_CUDA(cudaMemsetAsync(d_readout, 0, sizeof(double) * (size_t)ntraj * T_max, st));
+    if (d_final) SSS_CUDA(cudaMemsetAsync(d_final, 0, sizeof(double) * (size_t)ntraj * N, st));
+    p->last_launches = 0;
+    BatchLayout Ly;
+    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st)) return rc;
+    if (Ly.M == 0) return SSS_OK;
+    const int M = Ly.M, Ga = Ly.Ga, L = Ly.L, E = Ly.E, epl = Ly.epl, degree = Ly.degree,
+              substeps = Ly.substeps, threads = Ly.threads;
+    const bool use_reg = Ly.use_reg;
+    const long nnz = Ly.nnz;
+    const std::vector<int>& active = Ly.active;
+    const std::vector<int>& row_orig = Ly.row_orig;
+    std::vector<double> rw(M, 0.0);
+    if (h_rw)
+        for (int k = 0; k < M; k++) rw[k] = h_rw[row_orig[k]];
+    std::vector<double> toff(F), noff(p->d.Q);
+    for (int r = 0; r < F; r++) toff[r] = ((double)r * dt) / F;
+    for (int k = 0; k < p->d.Q; k++) noff[k] = (dt * p->nodes[k]) / F;
+
+    std::vector<double> dbl(Ly.gv);
+    const std::vector<unsigned>& words = Ly.words;
+    std::vector<int> ints(Ly.cnt);  // entries per lane, then row_orig
     const size_t n_gv = dbl.size();
     dbl.insert(dbl.end(), rw.begin(), rw.end());
     dbl.insert(dbl.end(), toff.begin(), toff.end());

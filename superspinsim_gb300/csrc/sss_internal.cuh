@@ -45,6 +45,23 @@ struct SparseGenerators {
     std::vector<double> val;    // G*nnz, generator-major
 };
 
+// Host-side layout of the batched kernels: reachable rows, active
+// generators, rows split across L lanes, per-lane entry lists.
+struct BatchLayout {
+    struct Ent { int col; int q; };   // compressed column, index into SparseGenerators
+    int M = 0, Ga = 0, L = 0, E = 0, epl = 0, degree = 0, substeps = 0, threads = 0;
+    bool use_reg = false;
+    long nnz = 0;
+    std::vector<int> active;                 // active generator indices
+    std::vector<std::vector<Ent>> row_ents;  // per reachable row (reachable order)
+    std::vector<std::vector<int>> lane_of;   // rows (reachable order) of each lane
+    std::vector<int> newpos, row_orig;       // reachable -> lane order; lane order -> original
+    std::vector<double> gv;                  // Ga*E*L generator values [g][e][l]
+    std::vector<unsigned> words;             // E*L entry words [e][l]
+    std::vector<int> entry_q;                // E*L index into SparseGenerators (-1: padding)
+    std::vector<int> cnt;                    // entries of each lane
+};
+
 }  // namespace sss
 
 struct sss_plan {
@@ -87,4 +104,11 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
               double t0, double dt, int T_max, int F, const double* h_rw,
               double* d_readout, double* d_final, cudaStream_t st);
 int build_sparse(sss_plan* p);
+// sss_adjoint.cu
+int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+                const double* d_prog, double t0, double dt, int T, int F, const double* h_rw,
+                const double* h_tw, double* d_J, double* d_grad, cudaStream_t st);
+int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+                 const double* d_prog, double dt, int F, const std::vector<int>& force_active,
+                 bool allow_register, BatchLayout* out, cudaStream_t st);
 }  // namespace sss

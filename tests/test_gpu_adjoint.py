@@ -1,0 +1,107 @@
+"""Adjoint gradients (sss_adjoint_run) against central finite differences
+of the GPU forward and of the CPU oracle."""
+import numpy as np
+import pytest
+
+from conftest import load_case, quadrature
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+F_RES = 2.870e9 + 28.025e9*5e-3
+
+
+def _problem(seed=5, B=3, S=4, seg=2e-9, t_read=4e-9):
+    from superspinsim_gb300 import protocols
+    rng = np.random.default_rng(seed)
+    rabi = rng.uniform(5e6, 20e6, (B, S))
+    phase = rng.uniform(0, 2*np.pi, (B, S))
+    progs, dur = protocols.pulse_shapes(rabi, phase, seg, F_RES, 10/65.9, t_read)
+    return rabi, phase, progs, dur
+
+
+def _objective(name="nv7_n19"):
+    from superspinsim_gb300.adjoint import Objective
+    c = load_case(name)
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1
+    return Objective(c["generators"], c["vectorisation_map"], rho, [3, 4, 5], 65.9e6,
+                     number_of_fine_divisions=100), c, rho
+
+
+def test_adjoint_objective_matches_forward_and_fd():
+    from superspinsim_gb300.adjoint import trapezoid_weights
+    obj, c, rho = _objective()
+    rabi, phase, progs, dur = _problem()
+    dt = 1e-9
+    T = int(round(dur[0]/dt))
+    S = rabi.shape[1]
+    tw = trapezoid_weights(T, dt, int(round(S*2e-9/dt)) - 1, T - 1)
+    J, grad = obj.run(progs, dt, T, tw)
+    Jf = obj.forward_only(progs, dt, T, tw)
+    assert np.abs(J - Jf).max() <= 1e-13*np.abs(Jf).max()
+    # central differences of the GPU forward, all parameters in one batch
+    B = progs.shape[0]
+    pert, idx = [], []
+    for b in range(B):
+        for s in range(S):
+            for kind, col, h in (("amp", 2, 1e-6*progs[b, 0, s, 2]), ("ph", 4, 1e-6)):
+                for sign in (1, -1):
+                    p = progs[b].copy()
+                    p[0, s, col] += sign*h
+                    pert.append(p)
+                idx.append((b, s, 0 if kind == "amp" else 1, h))
+    Jp = obj.forward_only(np.stack(pert), dt, T, tw)
+    for k, (b, s, comp, h) in enumerate(idx):
+        fd = (Jp[2*k] - Jp[2*k + 1])/(2*h)
+        scale = max(abs(fd), 1e-3*np.abs(grad[b, :S, comp]).max())
+        assert abs(grad[b, s, comp] - fd) <= 1e-6*scale, (b, s, comp, grad[b, s, comp], fd)
+
+
+def test_adjoint_matches_fd_of_oracle():
+    """Finite differences of the CPU oracle (the reference's integrator) on
+    one shape with two segments."""
+    from superspinsim_gb300.adjoint import trapezoid_weights
+    obj, c, rho = _objective()
+    rabi, phase, progs, dur = _problem(seed=9, B=1, S=2, seg=1e-9, t_read=2e-9)
+    dt = 1e-9
+    T = int(round(dur[0]/dt))
+    tw = trapezoid_weights(T, dt, 1, T - 1)
+    J, grad = obj.run(progs, dt, T, tw)
+    W, nodes = quadrature(2)
+    vm = c["vectorisation_map"]
+
+    def J_oracle(p):
+        _, d = oracle.simulate(c["generators"], rho, 0.0, T*dt + 1e-13, dt, p, K=2, W=W,
+                               nodes=nodes, F=100, vectorisation_map=vm, mode="vector",
+                               degree=16, flat_out=True)
+        return float((d @ obj.rw) @ tw)
+
+    assert abs(J_oracle(progs[0]) - J[0]) <= 1e-12*abs(J[0])
+    for s in range(2):
+        for comp, col, h in ((0, 2, 1e-6*progs[0, 0, s, 2]), (1, 4, 1e-6)):
+            pp, pm = progs[0].copy(), progs[0].copy()
+            pp[0, s, col] += h
+            pm[0, s, col] -= h
+            fd = (J_oracle(pp) - J_oracle(pm))/(2*h)
+            assert abs(grad[0, s, comp] - fd) <= 1e-5*abs(fd) + 1e-9*abs(J[0]), (s, comp)
+
+
+def test_torch_autograd_function():
+    torch = pytest.importorskip("torch")
+    from superspinsim_gb300.adjoint import make_pulse_function
+    obj, c, rho = _objective()
+    fn = make_pulse_function(obj, 2e-9, F_RES, 10/65.9, 4e-9, 1e-9)
+    rabi, phase, progs, dur = _problem(B=2, S=3)
+    r = torch.tensor(rabi, requires_grad=True)
+    p = torch.tensor(phase, requires_grad=True)
+    J = fn.apply(r, p)
+    J.sum().backward()
+    assert r.grad.shape == r.shape and p.grad.shape == p.shape
+    # one directional derivative against a forward difference pair
+    with torch.no_grad():
+        h = 1e-6
+        d = torch.zeros_like(p)
+        d[0, 1] = h
+        fd = (fn.apply(r, p + d) - fn.apply(r, p - d))[0]/(2*h)
+    assert abs(float(p.grad[0, 1]) - float(fd)) <= 1e-5*abs(float(fd)) + 1e-12
