@@ -40,22 +40,37 @@ def test_adjoint_objective_matches_forward_and_fd():
     J, grad = obj.run(progs, dt, T, tw)
     Jf = obj.forward_only(progs, dt, T, tw)
     assert np.abs(J - Jf).max() <= 1e-13*np.abs(Jf).max()
-    # central differences of the GPU forward, all parameters in one batch
+    # central differences of the GPU forward, all parameters in one batch,
+    # Richardson-extrapolated from steps h and 2h (h = 1e-3): truncation
+    # O(h^4) ~ 1e-12 and J's accumulated roundoff (~1e-14 relative) costs
+    # ~1e-11 of J per unit derivative -- both far below the tolerance
     B = progs.shape[0]
     pert, idx = [], []
     for b in range(B):
         for s in range(S):
-            for kind, col, h in (("amp", 2, 1e-6*progs[b, 0, s, 2]), ("ph", 4, 1e-6)):
-                for sign in (1, -1):
+            for comp, col, h in ((0, 2, 1e-3*progs[b, 0, s, 2]), (1, 4, 1e-3)):
+                for step in (h, -h, 2*h, -2*h):
                     p = progs[b].copy()
-                    p[0, s, col] += sign*h
+                    p[0, s, col] += step
                     pert.append(p)
-                idx.append((b, s, 0 if kind == "amp" else 1, h))
+                idx.append((b, s, comp, h))
     Jp = obj.forward_only(np.stack(pert), dt, T, tw)
     for k, (b, s, comp, h) in enumerate(idx):
-        fd = (Jp[2*k] - Jp[2*k + 1])/(2*h)
-        scale = max(abs(fd), 1e-3*np.abs(grad[b, :S, comp]).max())
-        assert abs(grad[b, s, comp] - fd) <= 1e-6*scale, (b, s, comp, grad[b, s, comp], fd)
+        d1 = (Jp[4*k] - Jp[4*k + 1])/(2*h)
+        d2 = (Jp[4*k + 2] - Jp[4*k + 3])/(4*h)
+        fd = (4*d1 - d2)/3
+        atol = 1e-11*abs(J[b])/h
+        assert abs(grad[b, s, comp] - fd) <= 1e-7*abs(fd) + atol, (b, s, comp, grad[b, s, comp], fd)
+    # and the plain central difference with h = 1e-6 (the workload's check)
+    for k, (b, s, comp, h) in enumerate(idx[:4]):
+        p1, p2 = progs[b].copy(), progs[b].copy()
+        hh = h*1e-3
+        col = 2 if comp == 0 else 4
+        p1[0, s, col] += hh
+        p2[0, s, col] -= hh
+        Jc = obj.forward_only(np.stack([p1, p2]), dt, T, tw)
+        fd = (Jc[0] - Jc[1])/(2*hh)
+        assert abs(grad[b, s, comp] - fd) <= 1e-5*abs(fd) + 1e-13*abs(J[b])/hh
 
 
 def test_adjoint_matches_fd_of_oracle():
