@@ -271,6 +271,57 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint_workload(args, rank, world):
+    """Adjoint gradients of integrated fluorescence for 256 seeded pulse
+    shapes (128 piecewise-constant segments of 2 ns, Rabi 0-20 MHz, phase
+    0-2pi, carrier at the ms=0 -> +1 line, B = 5 mT) followed by a 300 ns
+    laser readout: 556 ns = 111,200 steps at 5 ps per shape.  Times the
+    checkpointed adjoint (objective + 256 gradients per shape) against one
+    forward solve of the same batch."""
+    import torch
+    from superspinsim_gb300 import protocols
+    from superspinsim_gb300.adjoint import Objective, trapezoid_weights
+    gens, vm = nv7_model()
+    rng = np.random.default_rng(20260104)
+    B = args.n_traj or 256
+    S = 128
+    rabi = rng.uniform(0, 20e6, (B, S))
+    phase = rng.uniform(0, 2*np.pi, (B, S))
+    progs, dur = protocols.pulse_shapes(rabi, phase, 2e-9, F_RES, LASER, 300e-9)
+    T = int(round(dur[0]/DT_OUT))
+    tw = trapezoid_weights(T, DT_OUT, S*2 - 1, T - 1)
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1.0
+    obj = Objective(gens, vm, rho, [3, 4, 5], 65.9e6, number_of_exponentials=K_EXP,
+                    number_of_fine_divisions=F)
+    for _ in range(args.warmup):
+        obj.run(progs, DT_OUT, T, tw)
+    torch.cuda.synchronize()
+    fwd, adj = [], []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        obj.forward_only(progs, DT_OUT, T, tw)
+        fwd.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        J, grad = obj.run(progs, DT_OUT, T, tw)
+        adj.append(time.perf_counter() - t)
+    fwd_s, adj_s = statistics.median(fwd), statistics.median(adj)
+    steps = B*T*F
+    line = {"metric": "NV-7 pulse-shape adjoint gradients/s", "value": B/adj_s,
+            "unit": "gradients/s (256 parameters each)", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3*adj_s, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{B} pulse shapes x 128 segments of 2 ns + 300 ns readout, "
+                                   "NV-7, dt 5 ps (111,200 steps each)",
+                       "parameters_per_shape": 2*S, "traj_steps": steps},
+            "adjoint_over_forward": adj_s/fwd_s,
+            "forward_traj_steps_per_s": steps/fwd_s,
+            "adjoint_traj_steps_per_s": steps/adj_s,
+            "objective_mean": float(np.mean(J))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -283,12 +334,15 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="odmr", choices=["odmr", "ramsey", "nv21"])
+    ap.add_argument("--workload", default="odmr", choices=["odmr", "ramsey", "nv21", "adjoint"])
     ap.add_argument("--n-traj", type=int, default=0)
     args = ap.parse_args()
     rank, world = dist_setup()
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
+        return
+    if args.workload == "adjoint":
+        run_adjoint_workload(args, rank, world)
         return
 
     import torch

@@ -20,6 +20,10 @@
 //     g_e = sum_{a+b<=d-1} (u_a . z_b) / (a+b+1)!,
 //     u_a = (Omega^T)^a mu,  z_b = G Omega^b rho,
 // and the adjoint itself moves as mu <- sum_{a<=d} u_a / a!  (= E^T mu).
+// Both come from one series: g_e = rho^T L(Omega^T, G^T) mu, and the
+// block matrix [[Omega^T, G^T], [0, Omega^T]] applied to [0; mu] by Horner
+// (degree d) gives L(Omega^T, G^T) mu on top and E^T mu below -- per term
+// two transposed products with Omega and one with G, no dot products.
 //
 // Checkpointing: the forward pass keeps the state every C ~ sqrt(steps)
 // steps; the backward sweep recomputes one interval at a time (storing the
@@ -79,6 +83,8 @@ struct AdjArgs {
 
 __device__ __forceinline__ int wcol(unsigned w) { return (int)(w & 0xffffu); }
 __device__ __forceinline__ int wend(unsigned w) { return (int)(w >> 16); }
+// transposed-entry index flag: the x generator is non-zero at this entry
+constexpr int kHasG = 1 << 30;
 
 // x-channel segment at time t: index (or -1) and its parameters
 __device__ __forceinline__ int x_segment(const double* prog, int nseg, double t) {
@@ -122,10 +128,37 @@ struct Group {
         for (int e = 0; e < nET; e++) {
             unsigned w = s_tent[e * L + li];
             int q = s_tidx[e * L + li];
-            if (q >= 0) s = fma(Om[q], in[wcol(w)], s);
+            if (q >= 0) s = fma(Om[q & ~kHasG], in[wcol(w)], s);
             if (wend(w)) {
                 out[wend(w) - 1] = s;
                 s = 0.0;
+            }
+        }
+    }
+    // px_out = (Om^T px + G^T py)*scale, py_out = base + (Om^T py)*scale on
+    // this lane's rows (G^T values read through the same entry indices)
+    __device__ void trans_block(const double* Om, const double* Gv, const double* px,
+                                const double* py, double* px_out, double* py_out,
+                                const double* base, double scale) const {
+        double s1 = 0.0, s2 = 0.0;
+        for (int e = 0; e < nET; e++) {
+            unsigned w = s_tent[e * L + li];
+            int q = s_tidx[e * L + li];
+            if (q >= 0) {
+                const int c = wcol(w);
+                const bool has_g = (q & kHasG) != 0;
+                q &= ~kHasG;
+                const double o = Om[q], pyc = py[c];
+                s1 = fma(o, px[c], s1);
+                if (has_g) s1 = fma(Gv[q], pyc, s1);
+                s2 = fma(o, pyc, s2);
+            }
+            if (wend(w)) {
+                const int row = wend(w) - 1;
+                px_out[row] = s1 * scale;
+                py_out[row] = fma(s2, scale, base[row]);
+                s1 = 0.0;
+                s2 = 0.0;
             }
         }
     }
@@ -146,7 +179,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
     unsigned* s_tent = s_ent + (size_t)E * L;
     int* s_tidx = reinterpret_cast<int*>(s_tent + (size_t)ET * L);
     const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + 2 * (size_t)ET * L + 1) / 2;
-    const size_t per_slot = ((size_t)E * L + (size_t)(7 + d) * M + kMaxQ * kMaxG + 4 * kMaxQ) | 1;
+    const size_t per_slot = ((size_t)E * L + 7 * (size_t)M + kMaxQ * kMaxG + 4 * kMaxQ) | 1;
     const int slot = threadIdx.x / L, li = threadIdx.x % L;
     double* Om = smem + shared_words + slot * per_slot;
     double* v = Om + (size_t)E * L;      // state
@@ -156,8 +189,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
     double* mun = mu + M;
     double* u0 = mun + M;
     double* u1 = u0 + M;
-    double* z = u1 + M;                  // d*M
-    double* coef = z + (size_t)d * M;    // Q*Ga
+    double* coef = u1 + M;               // Q*Ga
     double* nd = coef + kMaxQ * kMaxG;   // per node: cos, -amp*sin, segment (as double), used
 
     for (int i = threadIdx.x; i < Ga * E * L; i += blockDim.x) s_gv[i] = a.gv[i];
@@ -306,48 +338,31 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
                     const double* s = st + ((n - n0) * K + e) * M;
                     for (int i = grp.r0; i < grp.r1; i++) v[i] = s[i];
                     grp.sync();
-                    // z_b = Gx Omega^b rho, b = 0..d-1
-                    const double* cur = v;
-                    double* nxt = bA;
-                    for (int bb = 0; bb < d; bb++) {
-                        // z_b = Gx cur
-                        {
-                            double acc = 0.0;
-                            for (int q = 0; q < grp.nE; q++) {
-                                unsigned w = s_ent[q * L + li];
-                                acc = fma(s_gv[((size_t)a.xg * E + q) * L + li], cur[wcol(w)], acc);
-                                if (wend(w)) {
-                                    z[(size_t)bb * M + wend(w) - 1] = acc;
-                                    acc = 0.0;
-                                }
-                            }
-                        }
-                        if (bb + 1 < d) {
-                            grp.fwd(Om, cur, nxt, nullptr, 0.0);
-                            grp.sync();
-                            cur = nxt;
-                            nxt = (nxt == bA) ? bB : bA;
-                        }
-                    }
-                    // u_a = (Om^T)^a mu; g and E^T mu
-                    for (int i = grp.r0; i < grp.r1; i++) {
-                        u0[i] = mu[i];
-                        mun[i] = mu[i];
-                    }
+                    // Transposed block series on [0; mu]:
+                    //   px <- (Om^T px + G^T py)/j,  py <- mu + (Om^T py)/j,
+                    // j = d..1; then py = E^T mu and px = L(Om^T, G^T) mu,
+                    // so g = rho_before . px.
+                    double* pxc = mun;   // zero on entry
+                    double* pyc = mu;
+                    double* pxn = u0;
+                    double* pyn = u1;
+                    for (int i = grp.r0; i < grp.r1; i++) mun[i] = 0.0;
                     grp.sync();
-                    double gpart = 0.0;
-                    double* uc = u0;
-                    double* un = u1;
-                    for (int aa = 0; aa < d; aa++) {
-                        for (int bb = 0; bb + aa <= d - 1; bb++)
-                            gpart = fma(a.fact_inv[aa + bb + 1], grp.dot(uc, z + (size_t)bb * M), gpart);
-                        grp.trans(Om, uc, un);
+                    for (int j = d; j >= 1; j--) {
+                        grp.trans_block(Om, s_gv + (size_t)a.xg * E * L, pxc, pyc, pxn, pyn, mu,
+                                        a.inv_j[j]);
                         grp.sync();
-                        for (int i = grp.r0; i < grp.r1; i++) mun[i] = fma(a.fact_inv[aa + 1], un[i], mun[i]);
-                        double* tmp = uc; uc = un; un = tmp;
+                        if (j == d) {
+                            // pxc/pyc were mun/mu; move to the ping-pong pair
+                            pxc = pxn; pyc = pyn;
+                            pxn = bA; pyn = bB;
+                        } else {
+                            double* t1 = pxc; pxc = pxn; pxn = t1;
+                            double* t2 = pyc; pyc = pyn; pyn = t2;
+                        }
                     }
-                    const double g = grp.sum(gpart);
-                    for (int i = grp.r0; i < grp.r1; i++) mu[i] = mun[i];
+                    const double g = grp.sum(grp.dot(v, pxc));
+                    for (int i = grp.r0; i < grp.r1; i++) mu[i] = pyc[i];
                     grp.sync();
                     if (li == 0) {
                         for (int k = 0; k < Q; k++) {
@@ -432,7 +447,12 @@ int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 unsigned w = j < (int)lst.size() ? (unsigned)lst[j].first : (unsigned)k;
                 if (j == n - 1) w |= (unsigned)(k + 1) << 16;
                 tent[(size_t)(e + j) * L + l] = w;
-                if (j < (int)lst.size()) tidx[(size_t)(e + j) * L + l] = lst[j].second.first * L + lst[j].second.second;
+                if (j < (int)lst.size()) {
+                    const int fe = lst[j].second.first, fl = lst[j].second.second;
+                    int q = fe * L + fl;
+                    if (Ly.gv[((size_t)xg * E + fe) * L + fl] != 0.0) q |= kHasG;
+                    tidx[(size_t)(e + j) * L + l] = q;
+                }
             }
             e += n;
         }
@@ -482,7 +502,7 @@ int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
     if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
     const int slots_per_cta = threads / L;
     const size_t shared_words = (size_t)Ly.Ga * E * L + M + ((size_t)E * L + 2 * (size_t)ET * L + 1) / 2;
-    const size_t per_slot = ((size_t)E * L + (size_t)(7 + d) * M + kMaxQ * kMaxG + 4 * kMaxQ) | 1;
+    const size_t per_slot = ((size_t)E * L + 7 * (size_t)M + kMaxQ * kMaxG + 4 * kMaxQ) | 1;
     const size_t smem = sizeof(double) * (shared_words + slots_per_cta * per_slot);
     if (smem > 227 * 1024) return fail(SSS_EINVAL, "adjoint kernel: shared memory per CTA too large");
     int grid = std::max(1, (ntraj + slots_per_cta - 1) / slots_per_cta);
