@@ -382,6 +382,128 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
     }
 }
 
+// Single-chain register variant: as k_batch_reg, but rows are not padded
+// and each row is one FMA chain closed by a single Horner FMA -- fewer FP64
+// instructions per term, longer dependent chains.
+template <int L, int EPL>
+__global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
+    extern __shared__ double smem[];
+    const int M = a.M, Ga = a.Ga;
+    const int slot = threadIdx.x / L, li = threadIdx.x % L;
+    const size_t per_slot = (3 * (size_t)M + kMaxQ * kMaxG) | 1;
+    double* v = smem + slot * per_slot;
+    double* bufA = v + M;
+    double* bufB = bufA + M;
+    double* coef = bufB + M;
+    double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
+    for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
+    unsigned ent[EPL];
+#pragma unroll
+    for (int e = 0; e < EPL; e++) ent[e] = __ldg(a.ent + (size_t)e * L + li);
+    const int nE = __ldg(a.lane_rows + li);
+    __syncthreads();
+
+    const unsigned lane_in_warp = threadIdx.x & 31;
+    const unsigned leader = lane_in_warp / L * L;
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    int b = -1, T_b = 0, t = 0, r = 0;
+    const double* prog = nullptr;
+    double om[EPL];
+
+    while (true) {
+        if (r == 0 && t >= T_b) {
+            if (b >= 0 && a.fin) {
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                    }
+            }
+            int nb = 0;
+            if (li == 0) nb = atomicAdd(a.queue, 1);
+            nb = __shfl_sync(gmask, nb, leader);
+            b = nb;
+            if (b >= a.ntraj) break;
+            T_b = a.samples ? a.samples[b] : a.T_max;
+            t = 0;
+            prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
+#pragma unroll
+            for (int e = 0; e < EPL; e++)
+                if (ent_end(ent[e])) {
+                    int row = ent_end(ent[e]) - 1;
+                    v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
+                }
+            __syncwarp(gmask);
+            if (T_b == 0) continue;
+        }
+        sample_coefficients(a, prog, t, r, li, L, coef);
+        __syncwarp(gmask);
+        for (int e_exp = a.K - 1; e_exp >= 0; e_exp--) {
+            double ag[kMaxG];
+            for (int g = 0; g < Ga; g++) {
+                double s = 0.0;
+                for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
+                ag[g] = s * a.h_sub;
+            }
+#pragma unroll
+            for (int e = 0; e < EPL; e++) om[e] = 0.0;
+            for (int g = 0; g < Ga; g++) {
+                const double c = ag[g];
+                if (c == 0.0) continue;
+                const double* gv = a.gv + (size_t)g * EPL * L + li;
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (e < nE) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);
+            }
+            for (int m = 0; m < a.substeps; m++) {
+                const double* cur = v;
+                double* nxt = bufA;
+                for (int j = a.degree; j >= 1; j--) {
+                    const double ij = a.inv_j[j];
+                    double s0 = 0.0;
+#pragma unroll
+                    for (int e = 0; e < EPL; e++) {
+                        if (e >= nE) break;
+                        s0 = fma(om[e], cur[ent_col(ent[e])], s0);
+                        if (ent_end(ent[e])) {
+                            int row = ent_end(ent[e]) - 1;
+                            nxt[row] = fma(s0, ij, v[row]);
+                            s0 = 0.0;
+                        }
+                    }
+                    __syncwarp(gmask);
+                    cur = nxt;
+                    nxt = (nxt == bufA) ? bufB : bufA;
+                }
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        v[row] = cur[row];
+                    }
+                __syncwarp(gmask);
+            }
+        }
+        if (++r == a.F) {
+            r = 0;
+            if (a.readout) {
+                double s = 0.0;
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        s = fma(s_rw[row], v[row], s);
+                    }
+#pragma unroll
+                for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+            }
+            t++;
+        }
+    }
+}
+
 template <class Kern>
 int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_per_cta,
            size_t smem, cudaStream_t st) {
@@ -406,7 +528,16 @@ int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_pe
 
 
 template <int L>
-int launch_reg(sss_plan* p, int epl, const BatchArgs& a, int threads, size_t smem, cudaStream_t st) {
+int launch_reg(sss_plan* p, int epl, const BatchArgs& a, int threads, size_t smem, cudaStream_t st,
+               bool one_chain) {
+    if (one_chain) {
+        switch (epl) {
+            case 8: return launch(p, k_batch_reg1<L, 8>, a, threads, threads / L, smem, st);
+            case 16: return launch(p, k_batch_reg1<L, 16>, a, threads, threads / L, smem, st);
+            case 32: return launch(p, k_batch_reg1<L, 32>, a, threads, threads / L, smem, st);
+            default: return launch(p, k_batch_reg1<L, 64>, a, threads, threads / L, smem, st);
+        }
+    }
     switch (epl) {
         case 8: return launch(p, k_batch_reg<L, 8>, a, threads, threads / L, smem, st);
         case 16: return launch(p, k_batch_reg<L, 16>, a, threads, threads / L, smem, st);
@@ -581,7 +712,8 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
         return std::make_pair((int)*std::max_element(load.begin(), load.end()),
                               std::function<int(int)>(cost));
     };
-    auto reg_try = assign(true);
+    const bool pad2 = p->batch_variant != 3;
+    auto reg_try = assign(pad2);
     if (allow_register && reg_try.first <= 64 && p->batch_variant != 2) {
         use_reg = true;
         epl = 8;
@@ -654,6 +786,7 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     const int M = Ly.M, Ga = Ly.Ga, L = Ly.L, E = Ly.E, epl = Ly.epl, degree = Ly.degree,
               substeps = Ly.substeps, threads = Ly.threads;
     const bool use_reg = Ly.use_reg;
+    const bool one_chain = p->batch_variant == 3;
     const long nnz = Ly.nnz;
     const std::vector<int>& active = Ly.active;
     const std::vector<int>& row_orig = Ly.row_orig;
@@ -711,12 +844,12 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
         const size_t smem = sizeof(double) * ((threads / L) * per_slot + M);
         if (smem > 227 * 1024) return fail(SSS_EINVAL, "batched kernel: shared memory per CTA too large");
         switch (L) {
-            case 1: rc = launch_reg<1>(p, epl, a, threads, smem, st); break;
-            case 2: rc = launch_reg<2>(p, epl, a, threads, smem, st); break;
-            case 4: rc = launch_reg<4>(p, epl, a, threads, smem, st); break;
-            case 8: rc = launch_reg<8>(p, epl, a, threads, smem, st); break;
-            case 16: rc = launch_reg<16>(p, epl, a, threads, smem, st); break;
-            default: rc = launch_reg<32>(p, epl, a, threads, smem, st); break;
+            case 1: rc = launch_reg<1>(p, epl, a, threads, smem, st, one_chain); break;
+            case 2: rc = launch_reg<2>(p, epl, a, threads, smem, st, one_chain); break;
+            case 4: rc = launch_reg<4>(p, epl, a, threads, smem, st, one_chain); break;
+            case 8: rc = launch_reg<8>(p, epl, a, threads, smem, st, one_chain); break;
+            case 16: rc = launch_reg<16>(p, epl, a, threads, smem, st, one_chain); break;
+            default: rc = launch_reg<32>(p, epl, a, threads, smem, st, one_chain); break;
         }
     } else {
         const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
@@ -742,7 +875,7 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     p->last_rows = M;
     p->last_nnz = (int)nnz;
     p->last_epl = E;
-    p->last_variant = use_reg ? 1 : 2;
+    p->last_variant = use_reg ? (one_chain ? 3 : 1) : 2;
     p->last_active = Ga;
     return rc;
 }

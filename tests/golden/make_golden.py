@@ -33,7 +33,6 @@ Run:  python tests/golden/make_golden.py            (about 5 minutes, 1 core)
 import math
 import os
 import sys
-import tempfile
 import time as _time
 
 import numpy as np
@@ -104,7 +103,11 @@ _SHIM = {
 
 
 def install_shim():
-    root = tempfile.mkdtemp(prefix="sss_shim_")
+    # the shim (and the HOME the reference's mesolve writes its temporary
+    # module under) live in tests/golden/.shim, which git ignores
+    root = os.path.join(HERE, ".shim")
+    os.makedirs(root, exist_ok=True)
+    os.environ["HOME"] = os.path.join(root, "home")
     for rel, text in _SHIM.items():
         path = os.path.join(root, rel)
         os.makedirs(os.path.dirname(path), exist_ok=True)
@@ -354,6 +357,32 @@ def save_nv21():
     print(f"nv21_n441: N={gens.shape[1]} {_time.time() - t:.1f} s", flush=True)
 
 
+def mesolve_case():
+    """A driven, damped qubit through the reference's QuTiP-style front end
+    (superspinsim/sugar.py:21-161), rotating frame (its default).  The jump
+    operators are static: the reference's time-dependent jump path wraps
+    its coefficient in a closure over a name it then rebinds to the closure
+    itself (sugar.py:124-135) and recurses without end."""
+    sz = np.diag([1.0, -1.0]).astype(complex)
+    sx = np.array([[0, 1], [1, 0]], complex)
+    sm = np.array([[0, 0], [1, 0]], complex)
+    H = [math.tau*30e6*sz/2,
+         [sx, lambda t: math.tau*4e6*math.cos(math.tau*30e6*t)]]
+    c_ops = [math.sqrt(2e6)*sm, math.sqrt(1e5)*sz]
+    rho0 = np.array([[1, 0], [0, 0]], complex)
+    return H, c_ops, rho0
+
+
+def save_mesolve():
+    from superspinsim import mesolve
+    H, c_ops, rho0 = mesolve_case()
+    t = _time.time()
+    _, d = mesolve(H, rho0, 0.0, 20e-9, 1e-9, c_ops=c_ops, number_of_exponentials=5,
+                   number_of_fine_divisions=10)
+    np.savez_compressed(os.path.join(HERE, "mesolve_qubit.npz"), density=d)
+    print(f"mesolve_qubit: {_time.time() - t:.1f} s", flush=True)
+
+
 def build_generators(c):
     from superspinsim.generate_generators import generate_atoms, \
         make_rotating
@@ -444,6 +473,8 @@ def main():
         save_case(c)
     if not only or "nv21_n441" in only:
         save_nv21()
+    if not only or "mesolve_qubit" in only:
+        save_mesolve()
 
 
 if __name__ == "__main__":

@@ -27,7 +27,8 @@ def _excited_weights(vmap):
 
 
 @pytest.mark.parametrize("name", ["nv7_n49", "nv7_n19"])
-@pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 2), (8, 2)])
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 2), (8, 2),
+                                           (0, 3), (32, 3)])
 def test_batch_odmr_against_oracle(name, lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method

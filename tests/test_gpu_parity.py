@@ -147,3 +147,15 @@ def test_simspins_front_end_matches_reference(name):
                     use_rotating=c["rot"], use_residual=c["res"],
                     use_incoherent=c["use_incoherent"])
     assert np.abs(d - ref["density"]).max() <= 1e-12
+
+
+def test_mesolve_front_end_matches_reference():
+    """QuTiP-style front end against the reference's mesolve (static jump
+    operators, rotating frame, CF6:5, F = 10)."""
+    from superspinsim_gb300.sugar import mesolve
+    c, mg = _case_by_name("qubit_couple")   # only for the module handle
+    H, c_ops, rho0 = mg.mesolve_case()
+    ref = load_case("mesolve_qubit")["density"]
+    _, d = mesolve(H, rho0, 0.0, 20e-9, 1e-9, c_ops=c_ops, number_of_exponentials=5,
+                   number_of_fine_divisions=10)
+    assert np.abs(d - ref).max() <= 1e-12
