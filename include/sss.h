@@ -140,6 +140,29 @@ int sss_batch_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                   const double* readout_weights, double* readout,
                   double* final_state, int host, void* cuda_stream);
 
+/* The batched run in two parts (no reference counterpart).
+ * sss_batch_prepare analyses the batch on the host -- active generators,
+ * rows reachable from rho0's support, lane layout, Taylor degree from the
+ * programs' amplitude bound -- and uploads the kernel's tables (device
+ * pointers; readout_weights is a host array of N or NULL).  The prepared
+ * state lives in the plan until the next prepare or batched run.
+ * sss_batch_launch then runs output samples [t_begin, t_begin + n_samples)
+ * of every trajectory, continuing in place from `state` (ntraj*N, device:
+ * in, the states at sample t_begin; out, the states after the chunk) and
+ * filling those columns of `readout` (ntraj*T_max, or NULL).  It does not
+ * allocate or synchronise with the host, so a sequence of launches can be
+ * captured in a CUDA graph; chunks make runs resumable.  Programs passed to
+ * a launch may change values but must keep the prepared batch's size,
+ * shape, dt and F, the same zero/non-zero channels, no larger amplitudes
+ * (the Taylor degree was chosen for them) and initial states within the
+ * prepared support. */
+int sss_batch_prepare(sss_plan* plan, int ntraj, const double* rho0, int nch,
+                      int nseg, const double* programs, double dt, int F,
+                      const double* readout_weights, void* cuda_stream);
+int sss_batch_launch(sss_plan* plan, double* state, const double* programs,
+                     const int* samples, double t0, int t_begin, int n_samples,
+                     int T_max, double* readout, void* cuda_stream);
+
 /* Adjoint gradients (no reference counterpart: the reference computes no
  * derivatives).  For each trajectory, the objective
  *   J = sum_t time_weights[t] * dot(readout_weights, state after sample t)

@@ -24,7 +24,8 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
 SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
            "sss_plan_set_batch_config", "sss_plan_batch_info",
-           "sss_fp64_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_last_error",
+           "sss_fp64_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
+           "sss_batch_launch", "sss_last_error",
            "sss_plan_destroy"]
 
 
@@ -77,6 +78,10 @@ def load(build_if_missing=True):
         L.sss_fp64_peak.argtypes = [dp, vp]
         L.sss_adjoint_run.argtypes = [vp, i, vp, i, i, vp, d, d, i, i, dp, dp, vp, vp, i, vp]
         L.sss_adjoint_run.restype = i
+        L.sss_batch_prepare.argtypes = [vp, i, vp, i, i, vp, d, i, dp, vp]
+        L.sss_batch_prepare.restype = i
+        L.sss_batch_launch.argtypes = [vp, vp, vp, vp, d, i, i, i, vp, vp]
+        L.sss_batch_launch.restype = i
         L.sss_fp64_peak.restype = i
         L.sss_last_error.restype = ctypes.c_char_p
         L.sss_plan_destroy.argtypes = [vp]
@@ -221,6 +226,21 @@ class Plan:
             dptr(rw), dptr(tw), J.ctypes.data_as(ctypes.c_void_p),
             grad.ctypes.data_as(ctypes.c_void_p), 1, stream))
         return J, grad
+
+    def batch_prepare(self, rho0_ptr, B, programs_ptr, nch, nseg, dt, F,
+                      readout_weights=None, stream=None):
+        """Analyse a batch (device pointers) and upload the kernel tables."""
+        rw = None if readout_weights is None else np.ascontiguousarray(
+            readout_weights, dtype=np.float64)
+        check(load().sss_batch_prepare(self._h, B, rho0_ptr, nch, nseg, programs_ptr,
+                                       float(dt), int(F), dptr(rw), stream))
+
+    def batch_launch(self, state_ptr, programs_ptr, t0, t_begin, n_samples, T_max,
+                     samples_ptr=None, readout_ptr=None, stream=None):
+        """Run output samples [t_begin, t_begin + n_samples) in place on state."""
+        check(load().sss_batch_launch(self._h, state_ptr, programs_ptr, samples_ptr, float(t0),
+                                      int(t_begin), int(n_samples), int(T_max), readout_ptr,
+                                      stream))
 
     def set_batch_config(self, lanes=0, cta_threads=0, variant=0):
         check(load().sss_plan_set_batch_config(self._h, int(lanes), int(cta_threads),

@@ -350,6 +350,29 @@ int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nse
     return SSS_OK;
 }
 
+int sss_batch_prepare(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                      const double* programs, double dt, int F, const double* readout_weights,
+                      void* stream) {
+    if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, 1, F, rho0)) return rc;
+    if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
+    if (p->rotating) return fail(SSS_EINVAL, "batched runs support the lab frame only");
+    if (ntraj == 0) return fail(SSS_EINVAL, "empty batch");
+    return batch_prepare(p, ntraj, rho0, nch, nseg, programs, dt, F, readout_weights,
+                         (cudaStream_t)stream);
+}
+
+int sss_batch_launch(sss_plan* p, double* state, const double* programs, const int* samples,
+                     double t0, int t_begin, int n_samples, int T_max, double* readout,
+                     void* stream) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (!p->batch_ready) return fail(SSS_EINVAL, "no prepared batch (call sss_batch_prepare)");
+    if (!state || !programs) return fail(SSS_EINVAL, "null state or programs");
+    if (t_begin < 0 || n_samples < 0 || t_begin + n_samples > T_max)
+        return fail(SSS_EINVAL, "need 0 <= t_begin and t_begin + n_samples <= T_max");
+    return batch_launch(p, state, programs, samples, t0, t_begin, n_samples, T_max, readout,
+                        (cudaStream_t)stream);
+}
+
 int sss_plan_last_launches(const sss_plan* p) { return p ? p->last_launches : 0; }
 
 // FP64 FMA throughput probe: every thread runs 8 independent DFMA chains.
@@ -431,7 +454,8 @@ void sss_plan_destroy(sss_plan* p) {
     DevBuf* bufs[] = {&p->d_gens, &p->d_dlast, &p->d_slast, &p->d_V, &p->d_Vinv,
                       &p->d_sp_rowptr, &p->d_sp_col, &p->d_sp_val, &p->d_row_map,
                       &p->w_prop, &p->w_in, &p->w_out, &p->w_prog, &p->w_tab, &p->w_aux,
-                      &p->w_queue, &p->w_ro, &p->w_fin, &p->w_samples, &p->w_status};
+                      &p->w_queue, &p->w_ro, &p->w_fin, &p->w_samples, &p->w_status,
+                      &p->w_state};
     for (DevBuf* b : bufs) b->release();
     if (p->ev_begin) cudaEventDestroy(p->ev_begin);
     if (p->ev_end) cudaEventDestroy(p->ev_end);

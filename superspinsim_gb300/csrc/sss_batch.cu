@@ -87,6 +87,7 @@ struct BatchArgs {
     int Ga;       // active generators
     int K, Q, F, nch, nseg, T_max, ntraj, degree, substeps, N;
     int E;        // entries per lane (max over lanes)
+    int t_begin, t_end;        // output samples of this launch
     double h_sub, t0, dt;
     int gen_index[kMaxG];      // active generator -> coefficient slot
     const double* toff;        // F: (r*dt)/F
@@ -97,11 +98,11 @@ struct BatchArgs {
     const int* lane_rows;      // L: entries of each lane
     const int* row_orig;       // M
     const double* rw;          // M readout weights (or null)
-    const double* rho0;        // ntraj*N
+    const double* rho0;        // ntraj*N  state at sample t_begin
     const double* prog;        // ntraj*nch*nseg*5
     const int* samples;        // ntraj or null
     double* readout;           // ntraj*T_max or null
-    double* fin;               // ntraj*N or null
+    double* fin;               // ntraj*N  state after the launch (may alias rho0), or null
     int* queue;
     double inv_j[kMaxTaylor + 1];
 };
@@ -171,13 +172,16 @@ __global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
                         a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
                     }
                 }
+            if (b >= 0 && a.readout)
+                for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
+                    a.readout[(size_t)b * a.T_max + tt] = 0.0;
             int nb = 0;
             if (li == 0) nb = atomicAdd(a.queue, 1);
             nb = __shfl_sync(gmask, nb, leader);
             b = nb;
             if (b >= a.ntraj) break;
-            T_b = a.samples ? a.samples[b] : a.T_max;
-            t = 0;
+            T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
+            t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
             for (int e = 0; e < nE; e++) {
                 unsigned w = s_ent[e * L + li];
@@ -187,7 +191,7 @@ __global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
                 }
             }
             __syncwarp(gmask);
-            if (T_b == 0) continue;
+            if (t >= T_b) continue;
         }
         sample_coefficients(a, prog, t, r, li, L, coef);
         __syncwarp(gmask);
@@ -296,13 +300,16 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
                         a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
                     }
             }
+            if (b >= 0 && a.readout)
+                for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
+                    a.readout[(size_t)b * a.T_max + tt] = 0.0;
             int nb = 0;
             if (li == 0) nb = atomicAdd(a.queue, 1);
             nb = __shfl_sync(gmask, nb, leader);
             b = nb;
             if (b >= a.ntraj) break;
-            T_b = a.samples ? a.samples[b] : a.T_max;
-            t = 0;
+            T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
+            t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
 #pragma unroll
             for (int e = 0; e < EPL; e++)
@@ -311,7 +318,7 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
                     v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
                 }
             __syncwarp(gmask);
-            if (T_b == 0) continue;
+            if (t >= T_b) continue;
         }
         sample_coefficients(a, prog, t, r, li, L, coef);
         __syncwarp(gmask);
@@ -420,13 +427,16 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
                         a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
                     }
             }
+            if (b >= 0 && a.readout)
+                for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
+                    a.readout[(size_t)b * a.T_max + tt] = 0.0;
             int nb = 0;
             if (li == 0) nb = atomicAdd(a.queue, 1);
             nb = __shfl_sync(gmask, nb, leader);
             b = nb;
             if (b >= a.ntraj) break;
-            T_b = a.samples ? a.samples[b] : a.T_max;
-            t = 0;
+            T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
+            t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
 #pragma unroll
             for (int e = 0; e < EPL; e++)
@@ -435,7 +445,7 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
                     v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
                 }
             __syncwarp(gmask);
-            if (T_b == 0) continue;
+            if (t >= T_b) continue;
         }
         sample_coefficients(a, prog, t, r, li, L, coef);
         __syncwarp(gmask);
@@ -772,17 +782,23 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
     return SSS_OK;
 }
 
-int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,
-              const int* d_samples, const int* h_samples, double t0, double dt, int T_max, int F,
-              const double* h_rw, double* d_readout, double* d_final, cudaStream_t st) {
-    (void)h_samples;
+int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st) {
     const int N = p->d.N;
-    if (d_readout) SSS_CUDA(cudaMemsetAsync(d_readout, 0, sizeof(double) * (size_t)ntraj * T_max, st));
-    if (d_final) SSS_CUDA(cudaMemsetAsync(d_final, 0, sizeof(double) * (size_t)ntraj * N, st));
-    p->last_launches = 0;
+    p->batch_ready = false;
+    p->batch_empty = false;
     BatchLayout Ly;
     if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st)) return rc;
-    if (Ly.M == 0) return SSS_OK;
+    if (Ly.M == 0) {
+        p->batch_ready = true;
+        p->batch_empty = true;
+        p->batch_ntraj = ntraj;
+        p->batch_nch = nch;
+        p->batch_nseg = nseg;
+        p->batch_dt = dt;
+        p->batch_F = F;
+        return SSS_OK;
+    }
     const int M = Ly.M, Ga = Ly.Ga, L = Ly.L, E = Ly.E, epl = Ly.epl, degree = Ly.degree,
               substeps = Ly.substeps, threads = Ly.threads;
     const bool use_reg = Ly.use_reg;
@@ -821,9 +837,9 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
 
     BatchArgs a{};
     a.M = M; a.Ga = Ga; a.K = p->d.K; a.Q = p->d.Q; a.F = F; a.nch = nch; a.nseg = nseg;
-    a.T_max = T_max; a.ntraj = ntraj; a.degree = degree; a.substeps = substeps; a.N = N;
+    a.T_max = 0; a.ntraj = ntraj; a.degree = degree; a.substeps = substeps; a.N = N;
     a.E = E;
-    a.h_sub = dt / F / substeps; a.t0 = t0; a.dt = dt;
+    a.h_sub = dt / F / substeps; a.t0 = 0.0; a.dt = dt;
     for (int gi = 0; gi < Ga; gi++) a.gen_index[gi] = active[gi];
     a.W = p->d_gens.as<double>() + p->gens.size();
     a.gv = dv;
@@ -833,16 +849,77 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     a.ent = dw;
     a.lane_rows = di;
     a.row_orig = di + L;
-    a.rho0 = d_rho0; a.prog = d_prog; a.samples = d_samples;
-    a.readout = d_readout; a.fin = d_final;
+    a.rho0 = nullptr; a.prog = nullptr; a.samples = nullptr;
+    a.readout = nullptr; a.fin = nullptr;
     a.queue = p->w_queue.as<int>();
     for (int j = 0; j <= kMaxTaylor; j++) a.inv_j[j] = j ? 1.0 / j : 0.0;
 
-    int rc;
+    static_assert(sizeof(BatchArgs) <= sizeof(p->batch_args), "BatchArgs does not fit the plan");
+    memcpy(p->batch_args, &a, sizeof(BatchArgs));
+    p->batch_use_reg = use_reg;
+    p->batch_one_chain = one_chain;
+    p->batch_L = L;
+    p->batch_epl = epl;
+    p->batch_threads_used = threads;
+    p->batch_ntraj = ntraj;
+    p->batch_nch = nch;
+    p->batch_nseg = nseg;
+    p->batch_dt = dt;
+    p->batch_F = F;
+    p->batch_has_rw = h_rw != nullptr;
     if (use_reg) {
         const size_t per_slot = (3 * (size_t)M + kMaxQ * kMaxG) | 1;
-        const size_t smem = sizeof(double) * ((threads / L) * per_slot + M);
-        if (smem > 227 * 1024) return fail(SSS_EINVAL, "batched kernel: shared memory per CTA too large");
+        p->batch_smem = sizeof(double) * ((threads / L) * per_slot + M);
+    } else {
+        const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
+        const size_t per_slot = ((size_t)E * L + 3 * M + kMaxQ * kMaxG) | 1;
+        p->batch_smem = sizeof(double) * (shared_words + (threads / L) * per_slot);
+    }
+    if (p->batch_smem > 227 * 1024)
+        return fail(SSS_EINVAL, "batched kernel needs " + std::to_string(p->batch_smem) +
+                                    " bytes of shared memory per CTA (max 232448); use fewer "
+                                    "threads per CTA");
+    p->last_batch_lanes = L;
+    p->last_degree = degree;
+    p->last_substeps = substeps;
+    p->last_rows = M;
+    p->last_nnz = (int)nnz;
+    p->last_epl = E;
+    p->last_active = Ga;
+    p->last_variant = use_reg ? (one_chain ? 3 : 1) : 2;
+    p->batch_ready = true;
+    return SSS_OK;
+}
+
+int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
+                 double t0, int t_begin, int n_samples, int T_max, double* d_readout,
+                 cudaStream_t st) {
+    if (!p->batch_ready) return fail(SSS_EINVAL, "no prepared batch (call sss_batch_prepare)");
+    p->last_launches = 0;
+    if (p->batch_empty || n_samples <= 0) {
+        if (d_readout && n_samples > 0)
+            SSS_CUDA(cudaMemset2DAsync(d_readout + t_begin, sizeof(double) * T_max, 0,
+                                       sizeof(double) * n_samples, p->batch_ntraj, st));
+        return SSS_OK;
+    }
+    BatchArgs a;
+    memcpy(&a, p->batch_args, sizeof(BatchArgs));
+    a.rho0 = d_state;
+    a.fin = d_state;
+    a.prog = d_prog;
+    a.samples = d_samples;
+    a.readout = d_readout;
+    a.rw = d_readout ? a.rw : nullptr;
+    a.t0 = t0;
+    a.t_begin = t_begin;
+    a.t_end = t_begin + n_samples;
+    a.T_max = T_max;
+    SSS_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int), st));
+    const int L = p->batch_L, epl = p->batch_epl, threads = p->batch_threads_used;
+    const bool use_reg = p->batch_use_reg, one_chain = p->batch_one_chain;
+    const size_t smem = p->batch_smem;
+    int rc;
+    if (use_reg) {
         switch (L) {
             case 1: rc = launch_reg<1>(p, epl, a, threads, smem, st, one_chain); break;
             case 2: rc = launch_reg<2>(p, epl, a, threads, smem, st, one_chain); break;
@@ -852,13 +929,6 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
             default: rc = launch_reg<32>(p, epl, a, threads, smem, st, one_chain); break;
         }
     } else {
-        const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
-        const size_t per_slot = ((size_t)E * L + 3 * M + kMaxQ * kMaxG) | 1;
-        const size_t smem = sizeof(double) * (shared_words + (threads / L) * per_slot);
-        if (smem > 227 * 1024)
-            return fail(SSS_EINVAL, "batched kernel needs " + std::to_string(smem) +
-                                        " bytes of shared memory per CTA (max 232448); use fewer "
-                                        "threads per CTA");
         switch (L) {
             case 1: rc = launch(p, k_batch_lanes<1>, a, threads, threads, smem, st); break;
             case 2: rc = launch(p, k_batch_lanes<2>, a, threads, threads / 2, smem, st); break;
@@ -869,15 +939,25 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
         }
     }
     p->last_launches = rc == SSS_OK ? 1 : 0;
-    p->last_batch_lanes = L;
-    p->last_degree = degree;
-    p->last_substeps = substeps;
-    p->last_rows = M;
-    p->last_nnz = (int)nnz;
-    p->last_epl = E;
-    p->last_variant = use_reg ? (one_chain ? 3 : 1) : 2;
-    p->last_active = Ga;
     return rc;
+}
+
+int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,
+              const int* d_samples, const int* h_samples, double t0, double dt, int T_max, int F,
+              const double* h_rw, double* d_readout, double* d_final, cudaStream_t st) {
+    (void)h_samples;
+    const int N = p->d.N;
+    if (int rc = batch_prepare(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, h_rw, st)) return rc;
+    // the launch runs in place on a state buffer that starts as rho0
+    double* state = d_final;
+    if (!state) {
+        if (int rc = p->w_state.ensure(sizeof(double) * (size_t)ntraj * N)) return rc;
+        state = p->w_state.as<double>();
+    }
+    if (state != d_rho0)
+        SSS_CUDA(cudaMemcpyAsync(state, d_rho0, sizeof(double) * (size_t)ntraj * N,
+                                 cudaMemcpyDeviceToDevice, st));
+    return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st);
 }
 
 }  // namespace sss

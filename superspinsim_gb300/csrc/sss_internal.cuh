@@ -91,6 +91,15 @@ struct sss_plan {
     int num_sms = 0;
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // around the last batched kernel
     bool ev_recorded = false;
+    // prepared batch (sss_batch_prepare -> sss_batch_launch)
+    alignas(16) unsigned char batch_args[1024];
+    bool batch_ready = false, batch_empty = false, batch_use_reg = false,
+         batch_one_chain = false, batch_has_rw = false;
+    int batch_L = 0, batch_epl = 0, batch_threads_used = 0, batch_ntraj = 0, batch_nch = 0,
+        batch_nseg = 0, batch_F = 0;
+    double batch_dt = 0.0;
+    size_t batch_smem = 0;
+    sss::DevBuf w_state;
 };
 
 namespace sss {
@@ -108,6 +117,11 @@ int build_sparse(sss_plan* p);
 int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 const double* d_prog, double t0, double dt, int T, int F, const double* h_rw,
                 const double* h_tw, double* d_J, double* d_grad, cudaStream_t st);
+int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st);
+int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
+                 double t0, int t_begin, int n_samples, int T_max, double* d_readout,
+                 cudaStream_t st);
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
                  bool allow_register, BatchLayout* out, cudaStream_t st);

@@ -80,3 +80,103 @@ class Sweep:
 
     def info(self):
         return self.plan.batch_info()
+
+
+class ChunkedRun:
+    """A prepared batch on the GPU, run in chunks of output samples.
+
+    ``sss_batch_prepare`` analyses the batch once; every chunk is one
+    ``sss_batch_launch`` that continues in place from the device state
+    buffer, so a run can be stopped and resumed between chunks (``save`` /
+    ``load``), and the sequence of chunk launches can be captured once in a
+    CUDA graph and replayed (``replay``) for repeated sweeps whose inputs are
+    refreshed in the same device buffers.  Device buffers are torch tensors.
+    """
+
+    def __init__(self, sweep, rho0, programs, time_start, time_step, T_max, samples=None,
+                 readout_weights=None):
+        import torch
+        self.torch = torch
+        self.sweep = sweep
+        progs = stack(programs) if isinstance(programs, (list, tuple)) else np.ascontiguousarray(
+            programs, dtype=np.float64)
+        flat = sweep.flatten(rho0)
+        if flat.shape[0] == 1 and progs.shape[0] > 1:
+            flat = np.repeat(flat, progs.shape[0], axis=0)
+        self.B, self.N = flat.shape
+        self.t0, self.dt, self.T_max = float(time_start), float(time_step), int(T_max)
+        dev = torch.device("cuda")
+        self.rho0 = torch.from_numpy(np.ascontiguousarray(flat)).to(dev)
+        self.state = self.rho0.clone()
+        self.programs = torch.from_numpy(progs).to(dev)
+        self.samples = None if samples is None else torch.from_numpy(
+            np.ascontiguousarray(samples, dtype=np.int32)).to(dev)
+        self.readout = None if readout_weights is None else torch.zeros(
+            (self.B, self.T_max), dtype=torch.float64, device=dev)
+        self.t_next = 0
+        self.graph = None
+        stream = torch.cuda.current_stream().cuda_stream
+        sweep.plan.batch_prepare(self.rho0.data_ptr(), self.B, self.programs.data_ptr(),
+                                 progs.shape[1], progs.shape[2], self.dt, sweep.F,
+                                 readout_weights, stream=stream)
+
+    def _launch(self, t_begin, n):
+        self.sweep.plan.batch_launch(
+            self.state.data_ptr(), self.programs.data_ptr(), self.t0, t_begin, n, self.T_max,
+            samples_ptr=None if self.samples is None else self.samples.data_ptr(),
+            readout_ptr=None if self.readout is None else self.readout.data_ptr(),
+            stream=self.torch.cuda.current_stream().cuda_stream)
+
+    def step(self, n_samples):
+        """Run the next n_samples output samples (all trajectories)."""
+        n = min(int(n_samples), self.T_max - self.t_next)
+        if n > 0:
+            self._launch(self.t_next, n)
+            self.t_next += n
+        return self.t_next
+
+    def run(self, chunk):
+        while self.t_next < self.T_max:
+            self.step(chunk)
+        return self
+
+    def capture(self, chunk):
+        """Capture the whole run, chunk by chunk, in one CUDA graph (the
+        state starts again from rho0 on every replay)."""
+        torch = self.torch
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(g, stream=side):
+                self.state.copy_(self.rho0)
+                for t in range(0, self.T_max, chunk):
+                    self._launch(t, min(chunk, self.T_max - t))
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = g
+        self.t_next = self.T_max
+        return self
+
+    def replay(self):
+        self.graph.replay()
+        return self
+
+    def save(self, path):
+        """Checkpoint: the device state, the next sample index and the
+        readouts so far."""
+        np.savez(path, state=self.state.cpu().numpy(), t_next=self.t_next,
+                 readout=None if self.readout is None else self.readout.cpu().numpy())
+
+    def load(self, path):
+        with np.load(path, allow_pickle=True) as z:
+            self.state.copy_(self.torch.from_numpy(z["state"]))
+            self.t_next = int(z["t_next"])
+            if self.readout is not None:
+                self.readout.copy_(self.torch.from_numpy(z["readout"]))
+        return self
+
+    def results(self):
+        out = {"final": self.state.cpu().numpy()}
+        if self.readout is not None:
+            out["readout"] = self.readout.cpu().numpy()
+        return out
