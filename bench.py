@@ -360,6 +360,10 @@ def main():
     sweep = Sweep(gens, vm, number_of_exponentials=K_EXP, number_of_fine_divisions=F,
                   lanes=args.lanes, cta_threads=args.threads, variant=args.variant)
     plan = sweep.plan
+    tuned = None
+    if not (args.lanes or args.threads or args.variant):
+        from superspinsim_gb300.tune import autotune
+        tuned = autotune(sweep, rho0, progs, DT_OUT, samples=samples)
 
     stream = torch.cuda.Stream()
     d_rho0 = torch.from_numpy(rho0).cuda()
@@ -446,6 +450,10 @@ def main():
                        "dt_s": DT_OUT/F, "samples": T, "fine_divisions": F,
                        "traj_steps_per_step": units_per_step,
                        "l2": "flushed between timed steps (256 MiB write)",
+                       "autotune": None if tuned is None else {
+                           "chosen": {"lanes": tuned["config"][0], "variant": tuned["config"][1],
+                                      "cta_threads": tuned["config"][2]},
+                           "trials": len(tuned["trials"])},
                        "kernel": {"lanes": info["lanes"], "taylor_degree": info["degree"],
                                   "substeps": info["substeps"], "rows": info["rows"],
                                   "nnz": info["nnz"]},

@@ -1,0 +1,84 @@
+"""Autotuner for the batched kernel.
+
+Times short prepared launches of the actual batch (a few output samples of
+every trajectory) for each candidate configuration -- lanes per trajectory,
+kernel variant (two FMA chains per row or one) and CTA size -- with CUDA
+events on the launch stream, keeps the fastest, and caches the choice per
+(model, batch size, fine steps) for the process.
+"""
+import itertools
+
+import numpy as np
+
+from superspinsim_gb300.program import Program, stack
+
+_CACHE = {}
+
+
+def _key(sweep, B, progs):
+    g = sweep.generators
+    active = tuple(bool(np.any(progs[:, c, :, 1:3] != 0)) for c in range(progs.shape[1]))
+    return (g.shape, float(np.abs(g).sum()), B, sweep.F, active)
+
+
+def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, repeats=2,
+             lanes=(0, 8, 16, 32), variants=(0, 3), threads=(64, 128), use_cache=True):
+    """Pick and set the fastest batch configuration for this sweep and batch.
+    Returns {"config": (lanes, variant, threads), "ms_per_traj_step": ...,
+    "trials": [...]}."""
+    import torch
+    progs = stack(programs) if isinstance(programs, (list, tuple)) and programs and \
+        isinstance(programs[0], Program) else np.ascontiguousarray(programs, dtype=np.float64)
+    flat = sweep.flatten(rho0)
+    if flat.shape[0] == 1 and progs.shape[0] > 1:
+        flat = np.repeat(flat, progs.shape[0], axis=0)
+    B = flat.shape[0]
+    key = _key(sweep, B, progs)
+    if use_cache and key in _CACHE:
+        best = _CACHE[key]
+        L, var, th = best["config"]
+        sweep.plan.set_batch_config(lanes=L, cta_threads=th, variant=var)
+        return best
+    dev = torch.device("cuda")
+    d_rho0 = torch.from_numpy(np.ascontiguousarray(flat)).to(dev)
+    state = d_rho0.clone()
+    d_prog = torch.from_numpy(progs).to(dev)
+    stream = torch.cuda.current_stream()
+    trials = []
+    for L, var, th in itertools.product(lanes, variants, threads):
+        if L and th % L:
+            continue
+        try:
+            sweep.plan.set_batch_config(lanes=L, cta_threads=th, variant=var)
+            sweep.plan.batch_prepare(d_rho0.data_ptr(), B, d_prog.data_ptr(), progs.shape[1],
+                                     progs.shape[2], time_step, sweep.F,
+                                     stream=stream.cuda_stream)
+        except Exception as e:  # a configuration that does not fit
+            trials.append({"config": (L, var, th), "error": str(e)})
+            continue
+        state.copy_(d_rho0)
+        sweep.plan.batch_launch(state.data_ptr(), d_prog.data_ptr(), 0.0, 0, 1, probe_samples,
+                                stream=stream.cuda_stream)
+        times = []
+        for _ in range(repeats):
+            state.copy_(d_rho0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sweep.plan.batch_launch(state.data_ptr(), d_prog.data_ptr(), 0.0, 0, probe_samples,
+                                    probe_samples, stream=stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        info = sweep.plan.batch_info()
+        trials.append({"config": (L, var, th), "ms": min(times), "lanes": info["lanes"]})
+    ok = [t for t in trials if "ms" in t]
+    if not ok:
+        raise RuntimeError("no batch configuration fits: " + str(trials))
+    best = min(ok, key=lambda t: t["ms"])
+    steps = B*probe_samples*sweep.F
+    result = {"config": best["config"], "ms_per_traj_step": best["ms"]/steps, "trials": trials}
+    L, var, th = best["config"]
+    sweep.plan.set_batch_config(lanes=L, cta_threads=th, variant=var)
+    _CACHE[key] = result
+    return result

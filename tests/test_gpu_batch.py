@@ -205,3 +205,23 @@ def test_chunked_runs_graph_replay_and_resume(tmp_path):
     r3 = resumed.results()
     assert np.array_equal(r3["readout"], one["readout"])
     assert np.array_equal(r3["final"], one["final"])
+
+
+def test_autotuner_picks_a_working_configuration():
+    pytest.importorskip("torch")
+    from superspinsim_gb300 import protocols
+    from superspinsim_gb300.sweep import Sweep, population_weights
+    from superspinsim_gb300.tune import autotune
+    c = load_case("nv7_n19")
+    vm = c["vectorisation_map"]
+    progs = protocols.odmr(2.870e9 + 28.025e9*5e-3 + np.linspace(-5e6, 5e6, 24), 5e6, 0.15)
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1
+    sw = Sweep(c["generators"], vm, number_of_exponentials=2, number_of_fine_divisions=20)
+    res = autotune(sw, rho, progs, 1e-9, probe_samples=1, repeats=1)
+    assert len([t for t in res["trials"] if "ms" in t]) >= 2
+    w = population_weights(vm, [3, 4, 5])
+    out = sw.run(rho, progs, 0.0, 3e-9 + 1e-13, 1e-9, readout_weights=w, final_state=True)
+    sw2 = Sweep(c["generators"], vm, number_of_exponentials=2, number_of_fine_divisions=20)
+    out2 = sw2.run(rho, progs, 0.0, 3e-9 + 1e-13, 1e-9, readout_weights=w, final_state=True)
+    assert np.abs(out["final"] - out2["final"]).max() <= 1e-13
