@@ -129,7 +129,9 @@ int sss_simulate_device(sss_plan* plan, int ntraj, const double* rho0, int nch,
  * trajectory b it writes readout[b*T_max + t] = dot(readout_weights, state)
  * (a linear functional such as a population or a fluorescence rate); after
  * its last sample the row is zero-padded.  final_state (ntraj*N) receives
- * each trajectory's last state (NULL to skip).
+ * each trajectory's last state (NULL to skip); trace (ntraj*T_max*N)
+ * receives the full state after every output sample (NULL to skip; zero
+ * after a trajectory's last sample).
  *   samples: ntraj output-sample counts (NULL: all T_max)
  *   host != 0: all pointers are host pointers (copied in and out within the
  *   call); host == 0: device pointers.
@@ -138,7 +140,8 @@ int sss_batch_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                   int nseg, const double* programs, const int* samples,
                   double t0, double dt, int T_max, int F,
                   const double* readout_weights, double* readout,
-                  double* final_state, int host, void* cuda_stream);
+                  double* final_state, double* trace, int host,
+                  void* cuda_stream);
 
 /* The batched run in two parts (no reference counterpart).
  * sss_batch_prepare analyses the batch on the host -- active generators,

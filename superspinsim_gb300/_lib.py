@@ -71,7 +71,7 @@ def load(build_if_missing=True):
         sim = [vp, i, dp, i, i, dp, dp, d, d, i, i, dp, vp]
         L.sss_simulate.argtypes = sim
         L.sss_simulate_device.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, vp, vp]
-        L.sss_batch_run.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, dp, vp, vp, i, vp]
+        L.sss_batch_run.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, dp, vp, vp, vp, i, vp]
         L.sss_plan_last_launches.argtypes = [vp]
         L.sss_plan_set_batch_config.argtypes = [vp, i, i, i]
         L.sss_plan_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, dp]
@@ -179,15 +179,16 @@ class Plan:
         return out
 
     def batch(self, rho0, programs, t0, dt, T_max, F, samples=None,
-              readout_weights=None, want_final=False, stream=None):
+              readout_weights=None, want_final=False, stream=None, want_trace=False):
         """Host-buffer batched run.  Returns (readout (B, T_max) or None,
-        final (B, N) or None)."""
+        final (B, N) or None[, trace (B, T_max, N)])."""
         rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
         programs = np.ascontiguousarray(programs, dtype=np.float64)
         B = rho0.shape[0]
         nch, nseg = programs.shape[1], programs.shape[2]
         ro = np.empty((B, T_max)) if readout_weights is not None else None
         fin = np.empty((B, self.N)) if want_final else None
+        tr = np.empty((B, T_max, self.N)) if want_trace else None
         rw = None if readout_weights is None else np.ascontiguousarray(
             readout_weights, dtype=np.float64)
         smp = None if samples is None else np.ascontiguousarray(samples, dtype=np.int32)
@@ -196,7 +197,10 @@ class Plan:
             programs.ctypes.data_as(ctypes.c_void_p), iptr(smp), float(t0), float(dt),
             int(T_max), int(F), dptr(rw),
             None if ro is None else ro.ctypes.data_as(ctypes.c_void_p),
-            None if fin is None else fin.ctypes.data_as(ctypes.c_void_p), 1, stream))
+            None if fin is None else fin.ctypes.data_as(ctypes.c_void_p),
+            None if tr is None else tr.ctypes.data_as(ctypes.c_void_p), 1, stream))
+        if want_trace:
+            return ro, fin, tr
         return ro, fin
 
     def batch_device(self, rho0_ptr, B, programs_ptr, nch, nseg, t0, dt, T_max,
@@ -207,7 +211,7 @@ class Plan:
             readout_weights, dtype=np.float64)
         check(load().sss_batch_run(self._h, B, rho0_ptr, nch, nseg, programs_ptr,
                                    samples_ptr, float(t0), float(dt), int(T_max),
-                                   int(F), dptr(rw), readout_ptr, final_ptr, 0, stream))
+                                   int(F), dptr(rw), readout_ptr, final_ptr, None, 0, stream))
 
     def adjoint(self, rho0, programs, t0, dt, T, F, readout_weights, time_weights, stream=None):
         """Host-buffer adjoint run.  Returns (J (B,), grad (B, nseg, 2))."""

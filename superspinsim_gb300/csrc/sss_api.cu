@@ -228,9 +228,10 @@ int sss_simulate_device(sss_plan* p, int ntraj, const double* rho0, int nch, int
 int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
                   const double* programs, const int* samples, double t0, double dt, int T_max,
                   int F, const double* readout_weights, double* readout, double* final_state,
-                  int host, void* stream) {
+                  double* trace, int host, void* stream) {
     if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, T_max, F,
-                           readout ? (const void*)readout : (const void*)final_state))
+                           readout ? (const void*)readout
+                                   : (final_state ? (const void*)final_state : (const void*)trace)))
         return rc;
     if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
     if (p->rotating) return fail(SSS_EINVAL, "batched runs support the lab frame only");
@@ -255,7 +256,7 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
     }
     const double *d_rho0 = rho0, *d_prog = programs;
     const int* d_samples = samples;
-    double *d_ro = readout, *d_fin = final_state;
+    double *d_ro = readout, *d_fin = final_state, *d_tr = trace;
     size_t nprog = (size_t)ntraj * nch * nseg * 5;
     if (host) {
         for (size_t i = 0; i < nprog; i++)
@@ -281,6 +282,10 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
             if (int rc = p->w_fin.ensure(sizeof(double) * (size_t)ntraj * N)) return rc;
             d_fin = p->w_fin.as<double>();
         }
+        if (trace) {
+            if (int rc = p->w_out.ensure(sizeof(double) * (size_t)ntraj * T_max * N)) return rc;
+            d_tr = p->w_out.as<double>();
+        }
     }
     // reachability needs rho0's support on the host
     std::vector<double> h_rho0((size_t)ntraj * N);
@@ -292,7 +297,7 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
     (void)h_rho0;
     int rc = batch_run(p, ntraj, d_rho0, nch, nseg, d_prog, d_samples,
                        samples ? h_samples.data() : nullptr, t0, dt, T_max, F, readout_weights,
-                       d_ro, d_fin, st);
+                       d_ro, d_fin, st, d_tr);
     if (rc) return rc;
     if (host) {
         if (readout)
@@ -300,6 +305,9 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
                                      cudaMemcpyDeviceToHost, st));
         if (final_state)
             SSS_CUDA(cudaMemcpyAsync(final_state, d_fin, sizeof(double) * (size_t)ntraj * N,
+                                     cudaMemcpyDeviceToHost, st));
+        if (trace)
+            SSS_CUDA(cudaMemcpyAsync(trace, d_tr, sizeof(double) * (size_t)ntraj * T_max * N,
                                      cudaMemcpyDeviceToHost, st));
         SSS_CUDA(cudaStreamSynchronize(st));
     }

@@ -103,6 +103,7 @@ struct BatchArgs {
     const int* samples;        // ntraj or null
     double* readout;           // ntraj*T_max or null
     double* fin;               // ntraj*N  state after the launch (may alias rho0), or null
+    double* trace;             // ntraj*T_max*N  state after every output sample, or null
     int* queue;
     double inv_j[kMaxTaylor + 1];
 };
@@ -241,6 +242,15 @@ __global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
         }
         if (++r == a.F) {
             r = 0;
+            if (a.trace) {
+                for (int e = 0; e < nE; e++) {
+                    unsigned w = s_ent[e * L + li];
+                    if (ent_end(w)) {
+                        int row = ent_end(w) - 1;
+                        a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
+                    }
+                }
+            }
             if (a.readout) {
                 double s = 0.0;
                 for (int e = 0; e < nE; e++) {
@@ -372,6 +382,14 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
         }
         if (++r == a.F) {
             r = 0;
+            if (a.trace) {
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
+                    }
+            }
             if (a.readout) {
                 double s = 0.0;
 #pragma unroll
@@ -497,6 +515,14 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
         }
         if (++r == a.F) {
             r = 0;
+            if (a.trace) {
+#pragma unroll
+                for (int e = 0; e < EPL; e++)
+                    if (ent_end(ent[e])) {
+                        int row = ent_end(ent[e]) - 1;
+                        a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
+                    }
+            }
             if (a.readout) {
                 double s = 0.0;
 #pragma unroll
@@ -893,7 +919,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
 
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st) {
+                 cudaStream_t st, double* d_trace) {
     if (!p->batch_ready) return fail(SSS_EINVAL, "no prepared batch (call sss_batch_prepare)");
     p->last_launches = 0;
     if (p->batch_empty || n_samples <= 0) {
@@ -909,6 +935,7 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
     a.prog = d_prog;
     a.samples = d_samples;
     a.readout = d_readout;
+    a.trace = d_trace;
     a.rw = d_readout ? a.rw : nullptr;
     a.t0 = t0;
     a.t_begin = t_begin;
@@ -944,9 +971,12 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
 
 int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,
               const int* d_samples, const int* h_samples, double t0, double dt, int T_max, int F,
-              const double* h_rw, double* d_readout, double* d_final, cudaStream_t st) {
+              const double* h_rw, double* d_readout, double* d_final, cudaStream_t st,
+              double* d_trace) {
     (void)h_samples;
     const int N = p->d.N;
+    if (d_trace)
+        SSS_CUDA(cudaMemsetAsync(d_trace, 0, sizeof(double) * (size_t)ntraj * T_max * N, st));
     if (int rc = batch_prepare(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, h_rw, st)) return rc;
     // the launch runs in place on a state buffer that starts as rho0
     double* state = d_final;
@@ -957,7 +987,7 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     if (state != d_rho0)
         SSS_CUDA(cudaMemcpyAsync(state, d_rho0, sizeof(double) * (size_t)ntraj * N,
                                  cudaMemcpyDeviceToDevice, st));
-    return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st);
+    return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st, d_trace);
 }
 
 }  // namespace sss

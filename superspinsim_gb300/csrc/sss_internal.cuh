@@ -111,7 +111,7 @@ int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
 int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
               const double* d_prog, const int* d_samples, const int* h_samples,
               double t0, double dt, int T_max, int F, const double* h_rw,
-              double* d_readout, double* d_final, cudaStream_t st);
+              double* d_readout, double* d_final, cudaStream_t st, double* d_trace = nullptr);
 int build_sparse(sss_plan* p);
 // sss_adjoint.cu
 int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
@@ -121,7 +121,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
                   const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st);
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st);
+                 cudaStream_t st, double* d_trace = nullptr);
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
                  bool allow_register, BatchLayout* out, cudaStream_t st);

@@ -39,6 +39,9 @@ from superspinsim_gb300.program import Program
 from superspinsim_gb300.quadratures import method
 
 
+PLAIN_MAX_N = 52   # dense shared-memory propagator path (csrc/sss_plain.cu)
+
+
 def number_of_samples(time_start, time_end, time_step):
     return int((time_end - time_start)/time_step)
 
@@ -202,6 +205,21 @@ def generate_simulator(
         if T <= 0:
             return time, np.zeros((0, n, n), dtype=np.complex128)
         flat0 = flatten_density(rho0, N, vmap)[None]
+        if N > PLAIN_MAX_N:
+            # larger than the dense shared-memory propagator path: the same
+            # integrator through the batched kernel, full state per sample
+            if use_rotating or expm != "taylor":
+                raise NotImplementedError(
+                    f"N = {N} > {PLAIN_MAX_N}: only the lab frame with expm='taylor' is "
+                    "supported at this size")
+            if not isinstance(sampler, (Program, np.ndarray)):
+                raise NotImplementedError(
+                    f"N = {N} > {PLAIN_MAX_N}: pass the coefficients as a Program")
+            prog = sampler.as_array() if isinstance(sampler, Program) else sampler
+            plan = plan_for(time_step/F)
+            _, _, tr = plan.batch(flat0, prog[None], time_start, time_step, T, F,
+                                  want_trace=True)
+            return time, unflatten_density(tr[0], n, vmap)
         plan = plan_for(time_step/F)
         if isinstance(sampler, Program):
             states = plan.simulate(flat0, sampler.as_array()[None], time_start, time_step, T, F)

@@ -225,3 +225,25 @@ def test_autotuner_picks_a_working_configuration():
     sw2 = Sweep(c["generators"], vm, number_of_exponentials=2, number_of_fine_divisions=20)
     out2 = sw2.run(rho, progs, 0.0, 3e-9 + 1e-13, 1e-9, readout_weights=w, final_state=True)
     assert np.abs(out["final"] - out2["final"]).max() <= 1e-13
+
+
+def test_dropin_simulate_nv21_uses_batched_trace():
+    """generate_simulator/simulate at N = 441 (beyond the dense plain path)
+    runs the batched kernel with a full-state trace; against the oracle."""
+    from superspinsim_gb300 import generate_simulator, protocols
+    from superspinsim_gb300.quadratures import method
+    c = load_case("nv21_n441")
+    gens, vm = c["generators"], c["vectorisation_map"]
+    f_res = 2.870e9 + 28.025e9*0.05
+    prog = protocols.odmr([f_res + 2e6], 5e6, 10/65.9)[0]
+    rho = np.zeros((21, 21), complex)
+    for k in range(3, 6):
+        rho[k, k] = 1/3
+    sim = generate_simulator(prog, gens, vm, number_of_exponentials=2,
+                             number_of_fine_divisions=50)
+    t, d = sim(rho, 0.0, 3e-9 + 1e-13, 1e-9)
+    W, nodes = method(2)
+    _, ref = oracle.simulate(gens, rho, 0.0, 3e-9 + 1e-13, 1e-9, prog, K=2, W=W, nodes=nodes,
+                             F=50, vectorisation_map=vm, mode="vector", degree=16)
+    assert d.shape == (3, 21, 21)
+    assert np.abs(d - ref).max() <= 1e-12
