@@ -184,29 +184,19 @@ class ClockSampler:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        backend = "nccl"
-        dist.init_process_group(backend=backend)
-    return rank, world
+    from superspinsim_gb300 import replicas
+    return replicas.init()
 
 
 def barrier(world):
     if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+        from superspinsim_gb300 import replicas
+        replicas.barrier()
 
 
 def max_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from superspinsim_gb300 import replicas
+    return replicas.max_over_ranks(x) if world > 1 else x
 
 
 def flops_per_traj_step(info, G, K):
