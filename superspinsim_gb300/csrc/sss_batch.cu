@@ -96,6 +96,7 @@ struct BatchArgs {
     const double* gv;          // Ga * E * L  generator values [g][e][l]
     const unsigned* ent;       // E * L  packed entry words [e][l]
     const int* lane_rows;      // L: entries of each lane
+    const int* rbeg;           // L+1: rows [rbeg[l], rbeg[l+1]) belong to lane l
     const int* row_orig;       // M
     const double* rw;          // M readout weights (or null)
     const double* rho0;        // ntraj*N  state at sample t_begin
@@ -269,28 +270,29 @@ __global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
     }
 }
 
-// Register variant (per-lane entry count <= EPL): the lane's assembled
-// Omega entries and packed words live in registers for the whole step, its
-// rows are padded to an even length and summed in two interleaved chains
-// (merged at the row end), and the unrolled entry loop exits at the lane's
-// own count.  Generator values stay in global memory (read once per
-// exponential, L1-resident).
+// Two-chain register variant: as k_batch_reg1, but each row's entries
+// (padded to an even count) are summed in two interleaved chains whose
+// partial sums are parked separately and merged in the closing loop --
+// twice the independent FMAs in flight per lane.
 template <int L, int EPL>
 __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
     extern __shared__ double smem[];
     const int M = a.M, Ga = a.Ga;
     const int slot = threadIdx.x / L, li = threadIdx.x % L;
-    const size_t per_slot = (3 * (size_t)M + kMaxQ * kMaxG) | 1;
+    const size_t per_slot = (5 * (size_t)M + kMaxQ * kMaxG) | 1;
     double* v = smem + slot * per_slot;
     double* bufA = v + M;
     double* bufB = bufA + M;
-    double* coef = bufB + M;
+    double* rs0 = bufB + M;
+    double* rs1 = rs0 + M;
+    double* coef = rs1 + M;
     double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
     for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
     unsigned ent[EPL];
 #pragma unroll
     for (int e = 0; e < EPL; e++) ent[e] = __ldg(a.ent + (size_t)e * L + li);
     const int nE = __ldg(a.lane_rows + li);
+    const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
     __syncthreads();
 
     const unsigned lane_in_warp = threadIdx.x & 31;
@@ -302,14 +304,8 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
 
     while (true) {
         if (r == 0 && t >= T_b) {
-            if (b >= 0 && a.fin) {
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
-                    }
-            }
+            if (b >= 0 && a.fin)
+                for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
                     a.readout[(size_t)b * a.T_max + tt] = 0.0;
@@ -321,12 +317,7 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
-#pragma unroll
-            for (int e = 0; e < EPL; e++)
-                if (ent_end(ent[e])) {
-                    int row = ent_end(ent[e]) - 1;
-                    v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
-                }
+            for (int row = r0; row < r1; row++) v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
             __syncwarp(gmask);
             if (t >= T_b) continue;
         }
@@ -334,10 +325,20 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
         __syncwarp(gmask);
         for (int e_exp = a.K - 1; e_exp >= 0; e_exp--) {
             double ag[kMaxG];
-            for (int g = 0; g < Ga; g++) {
-                double s = 0.0;
-                for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
-                ag[g] = s * a.h_sub;
+            if (Ga <= L) {
+                double mine = 0.0;
+                if (li < Ga) {
+                    for (int k = 0; k < a.Q; k++)
+                        mine = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + li], mine);
+                    mine *= a.h_sub;
+                }
+                for (int g = 0; g < Ga; g++) ag[g] = __shfl_sync(gmask, mine, leader + g);
+            } else {
+                for (int g = 0; g < Ga; g++) {
+                    double s = 0.0;
+                    for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
+                    ag[g] = s * a.h_sub;
+                }
             }
 #pragma unroll
             for (int e = 0; e < EPL; e++) om[e] = 0.0;
@@ -361,43 +362,30 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
                         s0 = fma(om[e], cur[ent_col(ent[e])], s0);
                         s1 = fma(om[e + 1], cur[ent_col(ent[e + 1])], s1);
                         if (ent_end(ent[e + 1])) {
-                            int row = ent_end(ent[e + 1]) - 1;
-                            nxt[row] = fma(s0 + s1, ij, v[row]);
+                            const int row = ent_end(ent[e + 1]) - 1;
+                            rs0[row] = s0;
+                            rs1[row] = s1;
                             s0 = 0.0;
                             s1 = 0.0;
                         }
                     }
+                    for (int row = r0; row < r1; row++) nxt[row] = fma(rs0[row] + rs1[row], ij, v[row]);
                     __syncwarp(gmask);
                     cur = nxt;
                     nxt = (nxt == bufA) ? bufB : bufA;
                 }
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        v[row] = cur[row];
-                    }
+                for (int row = r0; row < r1; row++) v[row] = cur[row];
                 __syncwarp(gmask);
             }
         }
         if (++r == a.F) {
             r = 0;
-            if (a.trace) {
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
-                    }
-            }
+            if (a.trace)
+                for (int row = r0; row < r1; row++)
+                    a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
             if (a.readout) {
                 double s = 0.0;
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        s = fma(s_rw[row], v[row], s);
-                    }
+                for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
 #pragma unroll
                 for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
                 if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
@@ -407,25 +395,30 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
     }
 }
 
-// Single-chain register variant: as k_batch_reg, but rows are not padded
-// and each row is one FMA chain closed by a single Horner FMA -- fewer FP64
-// instructions per term, longer dependent chains.
+// Single-chain register variant.  Each row is one FMA chain; where a row
+// ends, its sum is parked in shared memory (a store, no FP64 issue slot),
+// and the lane closes its own rows with one Horner FMA each in a uniform
+// loop after the entries -- instead of a divergent FP64 block after every
+// entry position.  The per-exponential generator weights are computed once
+// per group (lane g computes weight g) and broadcast by shuffles.
 template <int L, int EPL>
 __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
     extern __shared__ double smem[];
     const int M = a.M, Ga = a.Ga;
     const int slot = threadIdx.x / L, li = threadIdx.x % L;
-    const size_t per_slot = (3 * (size_t)M + kMaxQ * kMaxG) | 1;
+    const size_t per_slot = (4 * (size_t)M + kMaxQ * kMaxG) | 1;
     double* v = smem + slot * per_slot;
     double* bufA = v + M;
     double* bufB = bufA + M;
-    double* coef = bufB + M;
+    double* rs = bufB + M;
+    double* coef = rs + M;
     double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
     for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
     unsigned ent[EPL];
 #pragma unroll
     for (int e = 0; e < EPL; e++) ent[e] = __ldg(a.ent + (size_t)e * L + li);
     const int nE = __ldg(a.lane_rows + li);
+    const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
     __syncthreads();
 
     const unsigned lane_in_warp = threadIdx.x & 31;
@@ -437,14 +430,8 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
 
     while (true) {
         if (r == 0 && t >= T_b) {
-            if (b >= 0 && a.fin) {
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
-                    }
-            }
+            if (b >= 0 && a.fin)
+                for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
                     a.readout[(size_t)b * a.T_max + tt] = 0.0;
@@ -456,12 +443,7 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
-#pragma unroll
-            for (int e = 0; e < EPL; e++)
-                if (ent_end(ent[e])) {
-                    int row = ent_end(ent[e]) - 1;
-                    v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
-                }
+            for (int row = r0; row < r1; row++) v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
             __syncwarp(gmask);
             if (t >= T_b) continue;
         }
@@ -469,10 +451,20 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
         __syncwarp(gmask);
         for (int e_exp = a.K - 1; e_exp >= 0; e_exp--) {
             double ag[kMaxG];
-            for (int g = 0; g < Ga; g++) {
-                double s = 0.0;
-                for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
-                ag[g] = s * a.h_sub;
+            if (Ga <= L) {
+                double mine = 0.0;
+                if (li < Ga) {
+                    for (int k = 0; k < a.Q; k++)
+                        mine = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + li], mine);
+                    mine *= a.h_sub;
+                }
+                for (int g = 0; g < Ga; g++) ag[g] = __shfl_sync(gmask, mine, leader + g);
+            } else {
+                for (int g = 0; g < Ga; g++) {
+                    double s = 0.0;
+                    for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
+                    ag[g] = s * a.h_sub;
+                }
             }
 #pragma unroll
             for (int e = 0; e < EPL; e++) om[e] = 0.0;
@@ -495,42 +487,27 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
                         if (e >= nE) break;
                         s0 = fma(om[e], cur[ent_col(ent[e])], s0);
                         if (ent_end(ent[e])) {
-                            int row = ent_end(ent[e]) - 1;
-                            nxt[row] = fma(s0, ij, v[row]);
+                            rs[ent_end(ent[e]) - 1] = s0;
                             s0 = 0.0;
                         }
                     }
+                    for (int row = r0; row < r1; row++) nxt[row] = fma(rs[row], ij, v[row]);
                     __syncwarp(gmask);
                     cur = nxt;
                     nxt = (nxt == bufA) ? bufB : bufA;
                 }
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        v[row] = cur[row];
-                    }
+                for (int row = r0; row < r1; row++) v[row] = cur[row];
                 __syncwarp(gmask);
             }
         }
         if (++r == a.F) {
             r = 0;
-            if (a.trace) {
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
-                    }
-            }
+            if (a.trace)
+                for (int row = r0; row < r1; row++)
+                    a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
             if (a.readout) {
                 double s = 0.0;
-#pragma unroll
-                for (int e = 0; e < EPL; e++)
-                    if (ent_end(ent[e])) {
-                        int row = ent_end(ent[e]) - 1;
-                        s = fma(s_rw[row], v[row], s);
-                    }
+                for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
 #pragma unroll
                 for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
                 if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
@@ -847,6 +824,15 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     dbl.insert(dbl.end(), toff.begin(), toff.end());
     dbl.insert(dbl.end(), noff.begin(), noff.end());
     ints.insert(ints.end(), row_orig.begin(), row_orig.end());
+    const size_t o_rbeg = ints.size();
+    {
+        int k = 0;
+        ints.push_back(0);
+        for (int l = 0; l < L; l++) {
+            k += (int)Ly.lane_of[l].size();
+            ints.push_back(k);
+        }
+    }
     size_t bytes = sizeof(double) * dbl.size() + sizeof(unsigned) * words.size() + sizeof(int) * ints.size();
     if (int rc = p->d_sp_val.ensure(bytes + 64)) return rc;
     std::vector<char> blob(bytes);
@@ -875,6 +861,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     a.ent = dw;
     a.lane_rows = di;
     a.row_orig = di + L;
+    a.rbeg = di + o_rbeg;
     a.rho0 = nullptr; a.prog = nullptr; a.samples = nullptr;
     a.readout = nullptr; a.fin = nullptr;
     a.queue = p->w_queue.as<int>();
@@ -894,7 +881,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     p->batch_F = F;
     p->batch_has_rw = h_rw != nullptr;
     if (use_reg) {
-        const size_t per_slot = (3 * (size_t)M + kMaxQ * kMaxG) | 1;
+        const size_t per_slot = ((one_chain ? 4 : 5) * (size_t)M + kMaxQ * kMaxG) | 1;
         p->batch_smem = sizeof(double) * ((threads / L) * per_slot + M);
     } else {
         const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
