@@ -192,8 +192,12 @@ int sss_plan_last_launches(const sss_plan* plan);
  * trajectory (1, 2, 4, 8, 16, 32; 0 = automatic), CTA size (a multiple of
  * 32 up to 256; 0 = 64) and variant (0 = register variant when the
  * per-lane share fits, else shared memory; 1 = same as 0; 2 = always the
- * shared-memory variant; 3 = register variant with one FMA chain per row).  No reference counterpart (the reference's
- * launch shapes are fixed, generate_simulator.py:85-106). */
+ * shared-memory variant; 3 = register variant with one FMA chain per row;
+ * 4 = row-part variant: rows cut into parts of a few entries, each lane
+ * running C equal-length FMA chains, 8, 16 or 32 lanes, small patterns
+ * only -- SSS_EINVAL when the pattern does not fit).  No reference
+ * counterpart (the reference's launch shapes are fixed,
+ * generate_simulator.py:85-106). */
 int sss_plan_set_batch_config(sss_plan* plan, int lanes, int cta_threads,
                               int variant);
 

@@ -430,7 +430,7 @@ int sss_plan_set_batch_config(sss_plan* p, int lanes, int cta_threads, int varia
         return fail(SSS_EINVAL, "lanes must be 0 (automatic) or a power of two up to 32");
     if (cta_threads != 0 && (cta_threads < 32 || cta_threads > 256 || cta_threads % 32))
         return fail(SSS_EINVAL, "cta_threads must be 0 or a multiple of 32 in [32, 256]");
-    if (variant < 0 || variant > 3) return fail(SSS_EINVAL, "variant must be 0, 1, 2 or 3");
+    if (variant < 0 || variant > 4) return fail(SSS_EINVAL, "variant must be 0, 1, 2, 3 or 4");
     p->batch_lanes = lanes;
     p->batch_threads = cta_threads;
     p->batch_variant = variant;

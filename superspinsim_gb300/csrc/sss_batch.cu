@@ -81,6 +81,9 @@ int build_sparse(sss_plan* p) {
 namespace {
 
 constexpr int kMaxTaylor = 24;
+constexpr int kCloseMax = 8;   // close slots per lane in the row-part variant
+// (C parts per lane, P entries per part) shapes of the row-part kernel
+constexpr int kPartShapes[][2] = {{1, 4}, {2, 4}, {4, 4}, {2, 8}};
 
 struct BatchArgs {
     int M;        // state rows kept (reachable)
@@ -106,6 +109,11 @@ struct BatchArgs {
     double* fin;               // ntraj*N  state after the launch (may alias rho0), or null
     double* trace;             // ntraj*T_max*N  state after every output sample, or null
     int* queue;
+    // row-part variant
+    const int* pcol;           // C*P*L  column of each part entry [e][l] (M: the zero row)
+    const unsigned* cw;        // kCloseMax*L  close words [k][l]
+    const double* om0;         // K*C*P*L  folded L0 part of Omega per exponential, or null
+    int kc;                    // close slots per lane (max over lanes)
     double inv_j[kMaxTaylor + 1];
 };
 
@@ -517,6 +525,159 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
     }
 }
 
+// Row-part variant.  Every row of the pruned pattern is cut into parts of
+// at most P entries, and lane l of a group holds C parts: C independent FMA
+// chains of exactly P entries (short parts are padded with zero entries that
+// read the zero row M), issued interleaved, with no branch between entries.
+// Each row has one owner lane, which closes it after the parts are parked in
+// shared memory: next[row] = v[row] + (1/j)*sum(parts), one FMA per part,
+// through kc uniform close slots (a close word is row | part << 16 |
+// first << 31; padding slots write the sink row M+1).  The longest dependent
+// chain per Horner term is P + kc FMAs instead of the longest row, and every
+// lane runs the same straight-line code.  The state lives in three rotating
+// buffers per trajectory, so an exponential ends without a copy.  When L0 is
+// active its coefficient is identically 1 (lab frame), so its share of Omega
+// for each exponential is read from a host table (om0) instead of recomputed.
+template <int L, int C, int P>
+__global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
+    extern __shared__ double smem[];
+    constexpr int CP = C * P;
+    const int M = a.M, Ga = a.Ga;
+    const int Ms = M + 2;  // rows, the zero row M, the sink row M+1
+    const int slot = threadIdx.x / L, li = threadIdx.x % L;
+    const size_t per_slot = (3 * (size_t)Ms + L * C + 1 + kMaxQ * kMaxG) | 1;
+    double* sbuf = smem + slot * per_slot;
+    double* parts = sbuf + 3 * (size_t)Ms;
+    double* coef = parts + L * C + 1;
+    double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
+    for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
+    for (int i = li; i < 3 * Ms; i += L) sbuf[i] = 0.0;
+    for (int i = li; i < L * C + 1; i += L) parts[i] = 0.0;
+    int col[CP];
+#pragma unroll
+    for (int e = 0; e < CP; e++) col[e] = __ldg(a.pcol + (size_t)e * L + li);
+    unsigned cw[kCloseMax];
+#pragma unroll
+    for (int k = 0; k < kCloseMax; k++) cw[k] = __ldg(a.cw + (size_t)k * L + li);
+    const int kc = a.kc;
+    const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
+    const int g_first = a.om0 ? 1 : 0;
+    __syncthreads();
+
+    const unsigned lane_in_warp = threadIdx.x & 31;
+    const unsigned leader = lane_in_warp / L * L;
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    double* v = sbuf;
+    double* x = sbuf + Ms;
+    double* y = x + Ms;
+    int b = -1, T_b = 0, t = 0, r = 0;
+    const double* prog = nullptr;
+    double om[CP];
+
+    while (true) {
+        if (r == 0 && t >= T_b) {
+            if (b >= 0 && a.fin)
+                for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+            if (b >= 0 && a.readout)
+                for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
+                    a.readout[(size_t)b * a.T_max + tt] = 0.0;
+            int nb = 0;
+            if (li == 0) nb = atomicAdd(a.queue, 1);
+            nb = __shfl_sync(gmask, nb, leader);
+            b = nb;
+            if (b >= a.ntraj) break;
+            T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
+            t = a.t_begin;
+            prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
+            for (int row = r0; row < r1; row++) v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
+            __syncwarp(gmask);
+            if (t >= T_b) continue;
+        }
+        sample_coefficients(a, prog, t, r, li, L, coef);
+        __syncwarp(gmask);
+        for (int e_exp = a.K - 1; e_exp >= 0; e_exp--) {
+            double ag[kMaxG];
+            if (Ga <= L) {
+                double mine = 0.0;
+                if (li < Ga) {
+                    for (int k = 0; k < a.Q; k++)
+                        mine = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + li], mine);
+                    mine *= a.h_sub;
+                }
+                for (int g = 0; g < Ga; g++) ag[g] = __shfl_sync(gmask, mine, leader + g);
+            } else {
+                for (int g = 0; g < Ga; g++) {
+                    double s = 0.0;
+                    for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
+                    ag[g] = s * a.h_sub;
+                }
+            }
+            if (g_first) {
+                const double* o0 = a.om0 + (size_t)e_exp * CP * L + li;
+#pragma unroll
+                for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
+            } else {
+#pragma unroll
+                for (int e = 0; e < CP; e++) om[e] = 0.0;
+            }
+            for (int g = g_first; g < Ga; g++) {
+                const double c = ag[g];
+                if (c == 0.0) continue;
+                const double* gv = a.gv + (size_t)g * CP * L + li;
+#pragma unroll
+                for (int e = 0; e < CP; e++) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);
+            }
+            for (int m = 0; m < a.substeps; m++) {
+                double* cur = v;
+                double* nxt = x;
+                for (int j = a.degree; j >= 1; j--) {
+                    const double ij = a.inv_j[j];
+                    double s[C];
+#pragma unroll
+                    for (int c = 0; c < C; c++) s[c] = 0.0;
+#pragma unroll
+                    for (int q = 0; q < P; q++)
+#pragma unroll
+                        for (int c = 0; c < C; c++) s[c] = fma(om[c * P + q], cur[col[c * P + q]], s[c]);
+#pragma unroll
+                    for (int c = 0; c < C; c++) parts[li * C + c] = s[c];
+                    __syncwarp(gmask);
+                    double acc = 0.0;
+#pragma unroll
+                    for (int k = 0; k < kCloseMax; k++) {
+                        if (k >= kc) break;
+                        const unsigned w = cw[k];
+                        const int row = (int)(w & 0xffffu);
+                        const double base = (w >> 31) ? v[row] : acc;
+                        acc = fma(parts[(w >> 16) & 0x7fffu], ij, base);
+                        nxt[row] = acc;
+                    }
+                    __syncwarp(gmask);
+                    cur = nxt;
+                    nxt = (nxt == x) ? y : x;
+                }
+                // cur holds the new state: it becomes v, the old v a scratch buffer
+                if (cur == x) x = v; else y = v;
+                v = cur;
+            }
+        }
+        if (++r == a.F) {
+            r = 0;
+            if (a.trace)
+                for (int row = r0; row < r1; row++)
+                    a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
+            if (a.readout) {
+                double s = 0.0;
+                for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
+#pragma unroll
+                for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+            }
+            t++;
+        }
+    }
+}
+
 template <class Kern>
 int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_per_cta,
            size_t smem, cudaStream_t st) {
@@ -539,6 +700,17 @@ int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_pe
     return SSS_OK;
 }
 
+
+template <int L>
+int launch_parts(sss_plan* p, int C, int P, const BatchArgs& a, int threads, size_t smem,
+                 cudaStream_t st) {
+    static_assert(sizeof(kPartShapes) / sizeof(kPartShapes[0]) == 4, "one case per part shape");
+    if (C == 1 && P == 4) return launch(p, k_batch_parts<L, 1, 4>, a, threads, threads / L, smem, st);
+    if (C == 2 && P == 4) return launch(p, k_batch_parts<L, 2, 4>, a, threads, threads / L, smem, st);
+    if (C == 4 && P == 4) return launch(p, k_batch_parts<L, 4, 4>, a, threads, threads / L, smem, st);
+    if (C == 2 && P == 8) return launch(p, k_batch_parts<L, 2, 8>, a, threads, threads / L, smem, st);
+    return fail(SSS_EINVAL, "no row-part kernel for this shape");
+}
 
 template <int L>
 int launch_reg(sss_plan* p, int epl, const BatchArgs& a, int threads, size_t smem, cudaStream_t st,
@@ -591,6 +763,127 @@ static void choose_taylor(double beta, int forced_degree, int* degree, int* subs
     }
     *degree = best_d;
     *substeps = best_m;
+}
+
+// Row-part layout (k_batch_parts): rows cut into parts of at most P
+// entries, parts spread over the L*C lane slots, rows given to owner lanes
+// by longest-processing-time first on their close cost (one slot per part,
+// one for an empty row).  Picks the (C, P) shape with the fewest FP64
+// instructions per Horner term (C*P + kc), then the shortest dependent
+// chain (P + kc).
+static int layout_parts(sss_plan* p, int degree, int substeps, int L, int M, int Ga, long nnz,
+                        const std::vector<int>& rows_reached, BatchLayout* out) {
+    BatchLayout& Ly = *out;
+    const SparseGenerators& sp = p->sparse;
+    const std::vector<std::vector<BatchLayout::Ent>>& row_ents = Ly.row_ents;
+    if (L != 8 && L != 16 && L != 32)
+        return fail(SSS_EINVAL, "row-part variant needs 8, 16 or 32 lanes per trajectory");
+    const int threads = p->batch_threads > 0 ? p->batch_threads : 64;
+    if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
+    auto nparts = [&](int i, int P) { return ((int)row_ents[i].size() + P - 1) / P; };
+    // owners by LPT on close cost; returns kc
+    auto owners = [&](int P, std::vector<std::vector<int>>* own) {
+        std::vector<int> order(M);
+        std::iota(order.begin(), order.end(), 0);
+        auto cost = [&](int i) { return std::max(1, nparts(i, P)); };
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+        std::vector<int> load(L, 0);
+        own->assign(L, {});
+        for (int i : order) {
+            int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[l] += cost(i);
+            (*own)[l].push_back(i);
+        }
+        for (auto& o : *own) std::sort(o.begin(), o.end());
+        return *std::max_element(load.begin(), load.end());
+    };
+    int bC = 0, bP = 0, bkc = 0;
+    long best_cost = -1, best_path = 0;
+    for (const auto& sh : kPartShapes) {
+        const int C = sh[0], P = sh[1];
+        long total = 0;
+        for (int i = 0; i < M; i++) total += nparts(i, P);
+        if (total > (long)L * C) continue;
+        std::vector<std::vector<int>> own;
+        const int kc = owners(P, &own);
+        if (kc > kCloseMax) continue;
+        const long cost = C * P + kc, path = P + kc;
+        if (best_cost < 0 || cost < best_cost || (cost == best_cost && path < best_path)) {
+            best_cost = cost; best_path = path; bC = C; bP = P; bkc = kc;
+        }
+    }
+    if (best_cost < 0)
+        return fail(SSS_EINVAL, "row-part variant does not fit this pattern at " + std::to_string(L) +
+                                    " lanes per trajectory");
+    const int C = bC, P = bP, CP = C * P;
+    std::vector<std::vector<int>> own;
+    owners(P, &own);
+    // rows renumbered in owner order: lane l owns [rbeg[l], rbeg[l+1])
+    std::vector<int>& newpos = Ly.newpos;
+    std::vector<int>& row_orig = Ly.row_orig;
+    newpos.assign(M, 0);
+    row_orig.assign(M, 0);
+    {
+        int k = 0;
+        for (int l = 0; l < L; l++)
+            for (int i : own[l]) { newpos[i] = k; row_orig[k] = rows_reached[i]; k++; }
+    }
+    // parts in row order, part j -> lane j % L, chain j / L
+    Ly.pcol.assign((size_t)CP * L, M);
+    Ly.gv.assign((size_t)Ga * CP * L, 0.0);
+    std::vector<std::vector<int>> part_slots(M);  // per row: smem slot lane*C + c of each part
+    {
+        int j = 0;
+        for (int i = 0; i < M; i++) {
+            const auto& ents = row_ents[i];
+            const int n = (int)ents.size(), np = nparts(i, P);
+            int at = 0;
+            for (int q = 0; q < np; q++) {
+                const int len = n / np + (q < n % np ? 1 : 0);
+                const int lane = j % L, c = j / L;
+                for (int e = 0; e < len; e++) {
+                    const BatchLayout::Ent& en = ents[at + e];
+                    const size_t idx = (size_t)(c * P + e) * L + lane;
+                    Ly.pcol[idx] = newpos[en.col];
+                    for (int gi = 0; gi < Ga; gi++)
+                        Ly.gv[((size_t)gi * CP + c * P + e) * L + lane] =
+                            sp.val[(size_t)Ly.active[gi] * sp.nnz + en.q];
+                }
+                at += len;
+                part_slots[i].push_back(lane * C + c);
+                j++;
+            }
+        }
+    }
+    const unsigned zero_part = (unsigned)(L * C) << 16, first = 1u << 31;
+    Ly.cw.assign((size_t)kCloseMax * L, (unsigned)(M + 1) | zero_part | first);
+    for (int l = 0; l < L; l++) {
+        int k = 0;
+        for (int i : own[l]) {
+            const unsigned row = (unsigned)newpos[i];
+            if (part_slots[i].empty()) {
+                Ly.cw[(size_t)k++ * L + l] = row | zero_part | first;
+                continue;
+            }
+            for (size_t q = 0; q < part_slots[i].size(); q++)
+                Ly.cw[(size_t)k++ * L + l] =
+                    row | ((unsigned)part_slots[i][q] << 16) | (q == 0 ? first : 0u);
+        }
+    }
+    Ly.lane_of = own;
+    Ly.parts = true;
+    Ly.C = C;
+    Ly.P = P;
+    Ly.kc = bkc;
+    Ly.L = L;
+    Ly.E = CP;
+    Ly.use_reg = false;
+    Ly.epl = 0;
+    Ly.nnz = nnz;
+    Ly.degree = degree;
+    Ly.substeps = substeps;
+    Ly.threads = threads;
+    return SSS_OK;
 }
 
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
@@ -700,6 +993,9 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
         while (L < cap && (long)ntraj * L < want) L *= 2;
     }
     if (p->batch_lanes > 0) L = p->batch_lanes;
+    if (allow_register && p->batch_variant == 4)
+        return layout_parts(p, degree, substeps, p->batch_lanes > 0 ? L : std::max(L, 8), M, Ga,
+                            nnz, rows_reached, out);
     // ---- rows to lanes, balanced by entry count.  The register variant
     // pads each row to an even length (two chains); an empty row carries
     // zero entries so that it still closes ----
@@ -817,8 +1113,24 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     for (int k = 0; k < p->d.Q; k++) noff[k] = (dt * p->nodes[k]) / F;
 
     std::vector<double> dbl(Ly.gv);
-    const std::vector<unsigned>& words = Ly.words;
-    std::vector<int> ints(Ly.cnt);  // entries per lane, then row_orig
+    const std::vector<unsigned>& words = Ly.parts ? Ly.cw : Ly.words;
+    // entries per lane (or part columns), then row_orig
+    std::vector<int> ints(Ly.parts ? Ly.pcol : Ly.cnt);
+    const size_t n_lane_ints = ints.size();
+    // row-part variant: L0's share of Omega per exponential, as the kernel
+    // would form it (coefficient 1: weight sum(W[e,k]*1), times h, times L0)
+    const bool fold0 = Ly.parts && !active.empty() && active[0] == 0;
+    const size_t o_om0 = dbl.size();
+    if (fold0) {
+        const int CP = Ly.C * Ly.P;
+        const double h_sub = dt / F / substeps;
+        for (int e = 0; e < p->d.K; e++) {
+            double s = 0.0;
+            for (int k = 0; k < p->d.Q; k++) s = std::fma(p->W[e * p->d.Q + k], 1.0, s);
+            const double ag0 = s * h_sub;
+            for (int i = 0; i < CP * L; i++) dbl.push_back(ag0 * Ly.gv[i]);
+        }
+    }
     const size_t n_gv = dbl.size();
     dbl.insert(dbl.end(), rw.begin(), rw.end());
     dbl.insert(dbl.end(), toff.begin(), toff.end());
@@ -860,8 +1172,14 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     a.noff = a.toff + F;
     a.ent = dw;
     a.lane_rows = di;
-    a.row_orig = di + L;
+    a.row_orig = di + n_lane_ints;
     a.rbeg = di + o_rbeg;
+    if (Ly.parts) {
+        a.pcol = di;
+        a.cw = dw;
+        a.om0 = fold0 ? dv + o_om0 : nullptr;
+        a.kc = Ly.kc;
+    }
     a.rho0 = nullptr; a.prog = nullptr; a.samples = nullptr;
     a.readout = nullptr; a.fin = nullptr;
     a.queue = p->w_queue.as<int>();
@@ -871,6 +1189,9 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     memcpy(p->batch_args, &a, sizeof(BatchArgs));
     p->batch_use_reg = use_reg;
     p->batch_one_chain = one_chain;
+    p->batch_parts = Ly.parts;
+    p->batch_C = Ly.C;
+    p->batch_P = Ly.P;
     p->batch_L = L;
     p->batch_epl = epl;
     p->batch_threads_used = threads;
@@ -880,7 +1201,10 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     p->batch_dt = dt;
     p->batch_F = F;
     p->batch_has_rw = h_rw != nullptr;
-    if (use_reg) {
+    if (Ly.parts) {
+        const size_t per_slot = (3 * (size_t)(M + 2) + L * Ly.C + 1 + kMaxQ * kMaxG) | 1;
+        p->batch_smem = sizeof(double) * ((threads / L) * per_slot + M);
+    } else if (use_reg) {
         const size_t per_slot = ((one_chain ? 4 : 5) * (size_t)M + kMaxQ * kMaxG) | 1;
         p->batch_smem = sizeof(double) * ((threads / L) * per_slot + M);
     } else {
@@ -899,7 +1223,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     p->last_nnz = (int)nnz;
     p->last_epl = E;
     p->last_active = Ga;
-    p->last_variant = use_reg ? (one_chain ? 3 : 1) : 2;
+    p->last_variant = Ly.parts ? 4 : use_reg ? (one_chain ? 3 : 1) : 2;
     p->batch_ready = true;
     return SSS_OK;
 }
@@ -933,7 +1257,13 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
     const bool use_reg = p->batch_use_reg, one_chain = p->batch_one_chain;
     const size_t smem = p->batch_smem;
     int rc;
-    if (use_reg) {
+    if (p->batch_parts) {
+        switch (L) {
+            case 8: rc = launch_parts<8>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+            case 16: rc = launch_parts<16>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+            default: rc = launch_parts<32>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+        }
+    } else if (use_reg) {
         switch (L) {
             case 1: rc = launch_reg<1>(p, epl, a, threads, smem, st, one_chain); break;
             case 2: rc = launch_reg<2>(p, epl, a, threads, smem, st, one_chain); break;

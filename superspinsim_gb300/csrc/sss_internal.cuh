@@ -60,6 +60,11 @@ struct BatchLayout {
     std::vector<unsigned> words;             // E*L entry words [e][l]
     std::vector<int> entry_q;                // E*L index into SparseGenerators (-1: padding)
     std::vector<int> cnt;                    // entries of each lane
+    // row-part variant: C parts of P entries per lane, kc close slots
+    bool parts = false;
+    int C = 0, P = 0, kc = 0;
+    std::vector<int> pcol;                   // C*P*L part entry columns [e][l]
+    std::vector<unsigned> cw;                // kCloseMax*L close words [k][l]
 };
 
 }  // namespace sss
@@ -86,7 +91,8 @@ struct sss_plan {
     int batch_threads = 0;  // CTA size of the batched kernel, 0: 128
     int last_batch_lanes = 0, last_degree = 0, last_substeps = 0, last_rows = 0,
         last_nnz = 0, last_grid = 0, last_epl = 0, last_active = 0, last_variant = 0;
-    int batch_variant = 0;  // 0: register variant when it fits, 2: shared-memory variant
+    int batch_variant = 0;  // 0: register variant when it fits, 2: shared-memory variant,
+                            // 3: one-chain register variant, 4: row-part variant
     int device = 0;
     int num_sms = 0;
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // around the last batched kernel
@@ -94,7 +100,8 @@ struct sss_plan {
     // prepared batch (sss_batch_prepare -> sss_batch_launch)
     alignas(16) unsigned char batch_args[1024];
     bool batch_ready = false, batch_empty = false, batch_use_reg = false,
-         batch_one_chain = false, batch_has_rw = false;
+         batch_one_chain = false, batch_has_rw = false, batch_parts = false;
+    int batch_C = 0, batch_P = 0;
     int batch_L = 0, batch_epl = 0, batch_threads_used = 0, batch_ntraj = 0, batch_nch = 0,
         batch_nseg = 0, batch_F = 0;
     double batch_dt = 0.0;

@@ -2,7 +2,7 @@
 
 Times short prepared launches of the actual batch (a few output samples of
 every trajectory) for each candidate configuration -- lanes per trajectory,
-kernel variant (two FMA chains per row or one) and CTA size -- with CUDA
+kernel variant (two FMA chains per row, one, or row parts) and CTA size -- with CUDA
 events on the launch stream, keeps the fastest, and caches the choice per
 (model, batch size, fine steps) for the process.
 """
@@ -22,7 +22,7 @@ def _key(sweep, B, progs):
 
 
 def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, repeats=2,
-             lanes=(0, 8, 16, 32), variants=(0, 3), threads=(64, 128), use_cache=True):
+             lanes=(0, 8, 16, 32), variants=(0, 3, 4), threads=(64, 128), use_cache=True):
     """Pick and set the fastest batch configuration for this sweep and batch.
     Returns {"config": (lanes, variant, threads), "ms_per_traj_step": ...,
     "trials": [...]}."""

@@ -28,7 +28,7 @@ def _excited_weights(vmap):
 
 @pytest.mark.parametrize("name", ["nv7_n49", "nv7_n19"])
 @pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 2), (8, 2),
-                                           (0, 3), (32, 3)])
+                                           (0, 3), (32, 3), (0, 4), (8, 4), (16, 4), (32, 4)])
 def test_batch_odmr_against_oracle(name, lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
@@ -57,7 +57,8 @@ def test_batch_odmr_against_oracle(name, lanes, variant):
     assert np.abs(ro - ref @ w).max() <= 1e-12
 
 
-def test_batch_uneven_lengths_and_plain_agree():
+@pytest.mark.parametrize("variant", [0, 4])
+def test_batch_uneven_lengths_and_plain_agree(variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
     c = load_case("nv7_n49")
@@ -74,6 +75,7 @@ def test_batch_uneven_lengths_and_plain_agree():
     rho0 = np.stack([oracle.flatten(rho, vm, N)]*B)
     W, nodes = method(2)
     plan = _lib.Plan(c["generators"], W, nodes)
+    plan.set_batch_config(variant=variant)
     w = _excited_weights(vm)
     ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, samples=samples, readout_weights=w,
                          want_final=True)
@@ -103,7 +105,8 @@ def test_batch_empty_and_zero_state():
     assert ro.shape == (0, 3)
 
 
-def test_batch_ramsey_uneven_against_oracle():
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (16, 4), (32, 4)])
+def test_batch_ramsey_uneven_against_oracle(lanes, variant):
     """Uneven Ramsey protocol (laser init, pi/2 - tau - pi/2, laser readout)
     with per-trajectory lengths, against the oracle trajectory by trajectory."""
     from superspinsim_gb300 import _lib, protocols
@@ -126,6 +129,7 @@ def test_batch_ramsey_uneven_against_oracle():
     rho0 = np.stack([oracle.flatten(rho, vm, N)]*B)
     W, nodes = method(2)
     plan = _lib.Plan(c["generators"], W, nodes)
+    plan.set_batch_config(lanes=lanes, variant=variant, cta_threads=64)
     w = _excited_weights(vm)
     ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, samples=samples, readout_weights=w,
                          want_final=True)
@@ -157,13 +161,19 @@ def test_batch_nv21_against_oracle():
     ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, want_final=True)
     info = plan.batch_info()
     assert info["rows"] < N
+    # the row-part kernel is for small patterns: 1,475 entries do not fit
+    plan.set_batch_config(lanes=32, variant=4)
+    with pytest.raises(_lib.SSSError, match="row-part"):
+        plan.batch(rho0, progs, 0.0, dt, T, F, want_final=True)
+    plan.set_batch_config()
     _, ref = oracle.simulate(gens, np.stack([rho]*4), 0.0, T*dt + 1e-13, dt, progs, K=2, W=W,
                              nodes=nodes, F=F, vectorisation_map=vm, mode="vector", degree=16,
                              flat_out=True)
     assert np.abs(fin - ref[:, -1]).max() <= 1e-12
 
 
-def test_chunked_runs_graph_replay_and_resume(tmp_path):
+@pytest.mark.parametrize("variant", [0, 4])
+def test_chunked_runs_graph_replay_and_resume(tmp_path, variant):
     """Prepare once, launch in chunks: identical to the one-shot run; the
     chunk sequence captured in a CUDA graph replays to the same result; a
     run saved half-way and resumed finishes identically."""
@@ -185,6 +195,7 @@ def test_chunked_runs_graph_replay_and_resume(tmp_path):
     rho[1, 1] = 1
     w = population_weights(vm, [3, 4, 5])
     sw = Sweep(c["generators"], vm, number_of_exponentials=2, number_of_fine_divisions=20)
+    sw.plan.set_batch_config(variant=variant)
     one = sw.run(np.repeat(rho[None], B, axis=0), progs, 0.0, T*dt + 1e-13, dt, samples=samples,
                  readout_weights=w, final_state=True)
     run = ChunkedRun(sw, rho, progs, 0.0, dt, T, samples=samples, readout_weights=w).run(chunk=3)
