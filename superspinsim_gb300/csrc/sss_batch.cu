@@ -82,6 +82,7 @@ namespace {
 
 constexpr int kMaxTaylor = 24;
 constexpr int kCloseMax = 8;   // close slots per lane in the row-part variant
+constexpr int kRing = 16;      // fine steps of coefficients per refill (row-part variant)
 // (C parts per lane, P entries per part) shapes of the row-part kernel
 constexpr int kPartShapes[][2] = {{1, 4}, {2, 4}, {4, 4}, {2, 8}};
 
@@ -112,8 +113,10 @@ struct BatchArgs {
     // row-part variant
     const int* pcol;           // C*P*L  column of each part entry [e][l] (M: the zero row)
     const unsigned* cw;        // kCloseMax*L  close words [k][l]
-    const double* om0;         // K*C*P*L  folded L0 part of Omega per exponential, or null
+    const double* om0;         // K*C*P*L  constant part of Omega per exponential
     int kc;                    // close slots per lane (max over lanes)
+    int n_live;                // generators assembled per step (the others are in om0)
+    int live[kMaxG];           // their active-generator slots
     double inv_j[kMaxTaylor + 1];
 };
 
@@ -535,20 +538,26 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
 // first << 31; padding slots write the sink row M+1).  The longest dependent
 // chain per Horner term is P + kc FMAs instead of the longest row, and every
 // lane runs the same straight-line code.  The state lives in three rotating
-// buffers per trajectory, so an exponential ends without a copy.  When L0 is
-// active its coefficient is identically 1 (lab frame), so its share of Omega
-// for each exponential is read from a host table (om0) instead of recomputed.
+// buffers per trajectory, so an exponential ends without a copy.
+//
+// Omega = om0[e] + sum over live generators of a_g G_g: om0 (host table)
+// holds L0 (coefficient 1 in the lab frame) and every channel that is
+// constant over the batch.  The live coefficients are sampled for kRing fine
+// steps at a time, spread over the group's lanes (node values, then the CF
+// weights a_g = h sum_k W[e,k] c_k,g), into a per-trajectory ring in shared
+// memory, so a step pays the cosine of its drive only once per kRing steps.
 template <int L, int C, int P>
 __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
     extern __shared__ double smem[];
     constexpr int CP = C * P;
-    const int M = a.M, Ga = a.Ga;
+    const int M = a.M, NL = a.n_live, K = a.K, Q = a.Q;
     const int Ms = M + 2;  // rows, the zero row M, the sink row M+1
     const int slot = threadIdx.x / L, li = threadIdx.x % L;
-    const size_t per_slot = (3 * (size_t)Ms + L * C + 1 + kMaxQ * kMaxG) | 1;
+    const size_t per_slot = (3 * (size_t)Ms + L * C + 1 + (size_t)kRing * (Q + K) * NL) | 1;
     double* sbuf = smem + slot * per_slot;
     double* parts = sbuf + 3 * (size_t)Ms;
-    double* coef = parts + L * C + 1;
+    double* ringc = parts + L * C + 1;           // [s][k][live] node values
+    double* ring_ag = ringc + kRing * Q * NL;    // [s][e][live] CF weights
     double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
     for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
     for (int i = li; i < 3 * Ms; i += L) sbuf[i] = 0.0;
@@ -561,7 +570,6 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
     for (int k = 0; k < kCloseMax; k++) cw[k] = __ldg(a.cw + (size_t)k * L + li);
     const int kc = a.kc;
     const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
-    const int g_first = a.om0 ? 1 : 0;
     __syncthreads();
 
     const unsigned lane_in_warp = threadIdx.x & 31;
@@ -570,7 +578,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
     double* v = sbuf;
     double* x = sbuf + Ms;
     double* y = x + Ms;
-    int b = -1, T_b = 0, t = 0, r = 0;
+    int b = -1, T_b = 0, t = 0, r = 0, rp = kRing;
     const double* prog = nullptr;
     double om[CP];
 
@@ -588,42 +596,43 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             if (b >= a.ntraj) break;
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
+            rp = kRing;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
             for (int row = r0; row < r1; row++) v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
             __syncwarp(gmask);
             if (t >= T_b) continue;
         }
-        sample_coefficients(a, prog, t, r, li, L, coef);
-        __syncwarp(gmask);
-        for (int e_exp = a.K - 1; e_exp >= 0; e_exp--) {
-            double ag[kMaxG];
-            if (Ga <= L) {
-                double mine = 0.0;
-                if (li < Ga) {
-                    for (int k = 0; k < a.Q; k++)
-                        mine = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + li], mine);
-                    mine *= a.h_sub;
-                }
-                for (int g = 0; g < Ga; g++) ag[g] = __shfl_sync(gmask, mine, leader + g);
-            } else {
-                for (int g = 0; g < Ga; g++) {
-                    double s = 0.0;
-                    for (int k = 0; k < a.Q; k++) s = fma(__ldg(a.W + e_exp * a.Q + k), coef[k * Ga + g], s);
-                    ag[g] = s * a.h_sub;
-                }
+        if (rp == kRing) {
+            // node values of the live channels for fine steps (t, r) .. +kRing-1,
+            // node time ((t0 + (r*dt)/F) + dt*t) + (dt*node)/F, each op rounded
+            for (int i = li; i < kRing * Q * NL; i += L) {
+                const int s = i / (Q * NL), rem = i - s * Q * NL, k = rem / NL, gi = rem - k * NL;
+                const int rr = r + s, ts = t + rr / a.F, rs = rr % a.F;
+                const double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + rs)),
+                                                      __dmul_rn(a.dt, (double)ts)),
+                                            __ldg(a.noff + k));
+                const int g = a.gen_index[a.live[gi]];
+                ringc[i] = (g - 1 < a.nch) ? channel_value(prog, a.nseg, g - 1, tn) : 0.0;
             }
-            if (g_first) {
-                const double* o0 = a.om0 + (size_t)e_exp * CP * L + li;
-#pragma unroll
-                for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
-            } else {
-#pragma unroll
-                for (int e = 0; e < CP; e++) om[e] = 0.0;
+            __syncwarp(gmask);
+            for (int i = li; i < kRing * K * NL; i += L) {
+                const int s = i / (K * NL), rem = i - s * K * NL, e = rem / NL, gi = rem - e * NL;
+                double w = 0.0;
+                for (int k = 0; k < Q; k++)
+                    w = fma(__ldg(a.W + e * Q + k), ringc[(s * Q + k) * NL + gi], w);
+                ring_ag[i] = w * a.h_sub;
             }
-            for (int g = g_first; g < Ga; g++) {
-                const double c = ag[g];
+            __syncwarp(gmask);
+            rp = 0;
+        }
+        for (int e_exp = K - 1; e_exp >= 0; e_exp--) {
+            const double* o0 = a.om0 + (size_t)e_exp * CP * L + li;
+#pragma unroll
+            for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
+            for (int gi = 0; gi < NL; gi++) {
+                const double c = ring_ag[(rp * K + e_exp) * NL + gi];
                 if (c == 0.0) continue;
-                const double* gv = a.gv + (size_t)g * CP * L + li;
+                const double* gv = a.gv + (size_t)a.live[gi] * CP * L + li;
 #pragma unroll
                 for (int e = 0; e < CP; e++) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);
             }
@@ -661,6 +670,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                 v = cur;
             }
         }
+        rp++;
         if (++r == a.F) {
             r = 0;
             if (a.trace)
@@ -908,6 +918,30 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
                 if (q[0] == -INFINITY) continue;  // never matches
                 cmax[c + 1] = std::max(cmax[c + 1], std::fabs(q[1]) + std::fabs(q[2]));
             }
+    // channels holding one constant value for every trajectory at all times
+    // (every segment of zero amplitude with the same offset, the last one
+    // never ending): the row-part kernel folds them into the constant part
+    // of Omega
+    Ly.chan_const.assign(G, 0);
+    Ly.chan_value.assign(G, 0.0);
+    for (int c = 0; c < nch && c + 1 < G; c++) {
+        bool ok = ntraj > 0 && nseg > 0;
+        double val = 0.0;
+        for (int b = 0; b < ntraj && ok; b++) {
+            const double* seg = &h_prog[((size_t)b * nch + c) * nseg * 5];
+            if (!(seg[(size_t)(nseg - 1) * 5] == INFINITY)) ok = false;
+            for (int q = 0; q < nseg && ok; q++) {
+                const double* sq = seg + (size_t)q * 5;
+                if (sq[2] != 0.0 || !(sq[1] == sq[1])) ok = false;
+                else if (b == 0 && q == 0) val = sq[1];
+                else if (sq[1] != val) ok = false;
+            }
+        }
+        if (ok) {
+            Ly.chan_const[c + 1] = 1;
+            Ly.chan_value[c + 1] = val;
+        }
+    }
     std::vector<int> active;
     for (int g = 0; g < G; g++) {
         bool nonzero_gen = false;
@@ -1117,19 +1151,35 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     // entries per lane (or part columns), then row_orig
     std::vector<int> ints(Ly.parts ? Ly.pcol : Ly.cnt);
     const size_t n_lane_ints = ints.size();
-    // row-part variant: L0's share of Omega per exponential, as the kernel
-    // would form it (coefficient 1: weight sum(W[e,k]*1), times h, times L0)
-    const bool fold0 = Ly.parts && !active.empty() && active[0] == 0;
+    // row-part variant: the constant part of Omega per exponential -- L0
+    // (coefficient 1 in the lab frame) and the channels that are constant
+    // over the batch -- formed as the kernel would (weight sum_k W[e,k]*c,
+    // times h, times the generator, accumulated by FMA in generator order);
+    // the other active generators stay live in the kernel
+    std::vector<int> live;
     const size_t o_om0 = dbl.size();
-    if (fold0) {
+    if (Ly.parts) {
         const int CP = Ly.C * Ly.P;
         const double h_sub = dt / F / substeps;
-        for (int e = 0; e < p->d.K; e++) {
-            double s = 0.0;
-            for (int k = 0; k < p->d.Q; k++) s = std::fma(p->W[e * p->d.Q + k], 1.0, s);
-            const double ag0 = s * h_sub;
-            for (int i = 0; i < CP * L; i++) dbl.push_back(ag0 * Ly.gv[i]);
+        std::vector<double> om0((size_t)p->d.K * CP * L, 0.0);
+        for (int gi = 0; gi < Ga; gi++) {
+            const int g = active[gi];
+            if (g != 0 && !Ly.chan_const[g]) {
+                live.push_back(gi);
+                continue;
+            }
+            const double X = g == 0 ? 1.0 : Ly.chan_value[g];
+            for (int e = 0; e < p->d.K; e++) {
+                double s = 0.0;
+                for (int k = 0; k < p->d.Q; k++) s = std::fma(p->W[e * p->d.Q + k], X, s);
+                const double ag = s * h_sub;
+                for (int i = 0; i < CP * L; i++) {
+                    double& o = om0[(size_t)e * CP * L + i];
+                    o = std::fma(ag, Ly.gv[(size_t)gi * CP * L + i], o);
+                }
+            }
         }
+        dbl.insert(dbl.end(), om0.begin(), om0.end());
     }
     const size_t n_gv = dbl.size();
     dbl.insert(dbl.end(), rw.begin(), rw.end());
@@ -1177,8 +1227,10 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     if (Ly.parts) {
         a.pcol = di;
         a.cw = dw;
-        a.om0 = fold0 ? dv + o_om0 : nullptr;
+        a.om0 = dv + o_om0;
         a.kc = Ly.kc;
+        a.n_live = (int)live.size();
+        for (size_t i = 0; i < live.size(); i++) a.live[i] = live[i];
     }
     a.rho0 = nullptr; a.prog = nullptr; a.samples = nullptr;
     a.readout = nullptr; a.fin = nullptr;
@@ -1202,7 +1254,8 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     p->batch_F = F;
     p->batch_has_rw = h_rw != nullptr;
     if (Ly.parts) {
-        const size_t per_slot = (3 * (size_t)(M + 2) + L * Ly.C + 1 + kMaxQ * kMaxG) | 1;
+        const size_t per_slot = (3 * (size_t)(M + 2) + L * Ly.C + 1 +
+                                 (size_t)kRing * (p->d.Q + p->d.K) * live.size()) | 1;
         p->batch_smem = sizeof(double) * ((threads / L) * per_slot + M);
     } else if (use_reg) {
         const size_t per_slot = ((one_chain ? 4 : 5) * (size_t)M + kMaxQ * kMaxG) | 1;

@@ -65,6 +65,8 @@ struct BatchLayout {
     int C = 0, P = 0, kc = 0;
     std::vector<int> pcol;                   // C*P*L part entry columns [e][l]
     std::vector<unsigned> cw;                // kCloseMax*L close words [k][l]
+    std::vector<char> chan_const;            // per generator: its channel is batch-constant
+    std::vector<double> chan_value;          // that constant
 };
 
 }  // namespace sss
