@@ -10,8 +10,8 @@
 // (2R = 70 dense N x N squarings per exponential in the reference, :706-724
 // and :882-897), its action on the state is summed directly,
 //     v <- sum_{j=0..d} Omega^j v / j!   (m sub-steps of Omega/m),
-// with d and m chosen from a norm bound so the truncation stays below
-// 1e-18 per exponential.  Omega = h * sum_g a_g G_g is assembled only on
+// with d and m chosen from a norm bound so the truncation stays below the
+// unit roundoff 2^-53 per exponential.  Omega = h * sum_g a_g G_g is assembled only on
 // the union sparsity pattern of the generators that are active in the
 // batch (a generator whose coefficient is zero for every trajectory is
 // dropped), restricted to the state entries reachable from the initial
@@ -743,8 +743,14 @@ int launch_reg(sss_plan* p, int epl, const BatchArgs& a, int threads, size_t sme
 
 }  // namespace
 
+// Truncation tolerance of the Taylor series per exponential: the unit
+// roundoff 2^-53, the tolerance of the truncated-Taylor action of the
+// matrix exponential (Al-Mohy & Higham, SIAM J. Sci. Comput. 33(2), 2011).
+// The series error then stays below the rounding of a single step.
+constexpr double kTaylorTol = 0x1p-53;
+
 // Taylor degree and sub-steps for a norm bound `beta` of Omega: the
-// smallest d*m with m*(beta/m)^(d+1)/(d+1)! <= 1e-18.
+// smallest d*m with m*(beta/m)^(d+1)/(d+1)! <= kTaylorTol.
 static void choose_taylor(double beta, int forced_degree, int* degree, int* substeps) {
     if (forced_degree > 0) {
         *degree = std::min(forced_degree, kMaxTaylor);
@@ -752,7 +758,7 @@ static void choose_taylor(double beta, int forced_degree, int* degree, int* subs
         while (m < 1024) {
             double x = beta / m, term = 1.0;
             for (int j = 1; j <= *degree + 1; j++) term *= x / j;
-            if (m * term <= 1e-18) break;
+            if (m * term <= kTaylorTol) break;
             m++;
         }
         *substeps = m;
@@ -764,7 +770,7 @@ static void choose_taylor(double beta, int forced_degree, int* degree, int* subs
         for (int d = 1; d <= kMaxTaylor; d++) {
             term *= x / d;
             double next = term * x / (d + 1);
-            if (m * next <= 1e-18) {
+            if (m * next <= kTaylorTol) {
                 if (d * m < best_d * best_m) { best_d = d; best_m = m; }
                 break;
             }
