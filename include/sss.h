@@ -190,16 +190,25 @@ int sss_plan_last_launches(const sss_plan* plan);
 
 /* Batched-kernel configuration (the autotuner's knobs): lanes per
  * trajectory (1, 2, 4, 8, 16, 32; 0 = automatic), CTA size (a multiple of
- * 32 up to 256; 0 = 64) and variant (0 = register variant when the
- * per-lane share fits, else shared memory; 1 = same as 0; 2 = always the
- * shared-memory variant; 3 = register variant with one FMA chain per row;
- * 4 = row-part variant: rows cut into parts of a few entries, each lane
- * running C equal-length FMA chains, 8, 16 or 32 lanes, small patterns
- * only -- SSS_EINVAL when the pattern does not fit).  No reference
- * counterpart (the reference's launch shapes are fixed,
+ * 32 up to 256; 0 = 32 for the row-part variant, else 64) and variant
+ * (0 = automatic: the row-part variant when the pattern fits, else as 1;
+ * 1 = register variant when the per-lane share fits, else shared memory;
+ * 2 = always the shared-memory variant; 3 = register variant with one FMA
+ * chain per row; 4 = row-part variant: rows cut into parts of a few
+ * entries, each lane running C equal-length FMA chains, 8, 16 or 32 lanes,
+ * small patterns only -- SSS_EINVAL when the pattern does not fit).  No
+ * reference counterpart (the reference's launch shapes are fixed,
  * generate_simulator.py:85-106). */
 int sss_plan_set_batch_config(sss_plan* plan, int lanes, int cta_threads,
                               int variant);
+
+/* Device memory (bytes) sss_adjoint_run may use for the forward states it
+ * stores (the state before every exponential of every trajectory); 0 = half
+ * of the free device memory at the call.  Trajectories are processed in
+ * chunks that fit; when the states of one trajectory do not fit, the
+ * checkpointed adjoint (which recomputes intervals) runs instead.  No
+ * reference counterpart (the reference has no derivatives). */
+int sss_plan_set_adjoint_memory(sss_plan* plan, size_t max_bytes);
 
 /* What the last sss_batch_run used: lanes per trajectory, Taylor degree,
  * sub-steps per exponential, state rows kept after the reachability

@@ -23,7 +23,7 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
 
 SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
-           "sss_plan_set_batch_config", "sss_plan_batch_info",
+           "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
            "sss_fp64_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
            "sss_batch_launch", "sss_last_error",
            "sss_plan_destroy"]
@@ -74,6 +74,8 @@ def load(build_if_missing=True):
         L.sss_batch_run.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, dp, vp, vp, vp, i, vp]
         L.sss_plan_last_launches.argtypes = [vp]
         L.sss_plan_set_batch_config.argtypes = [vp, i, i, i]
+        L.sss_plan_set_adjoint_memory.argtypes = [vp, ctypes.c_size_t]
+        L.sss_plan_set_adjoint_memory.restype = i
         L.sss_plan_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, dp]
         L.sss_fp64_peak.argtypes = [dp, vp]
         L.sss_adjoint_run.argtypes = [vp, i, vp, i, i, vp, d, d, i, i, dp, dp, vp, vp, i, vp]
@@ -249,6 +251,11 @@ class Plan:
     def set_batch_config(self, lanes=0, cta_threads=0, variant=0):
         check(load().sss_plan_set_batch_config(self._h, int(lanes), int(cta_threads),
                                                int(variant)))
+
+    def set_adjoint_memory(self, max_bytes=0):
+        """Device memory the adjoint may use for stored forward states
+        (0: half of the free memory)."""
+        check(load().sss_plan_set_adjoint_memory(self._h, int(max_bytes)))
 
     def batch_info(self):
         vals = [ctypes.c_int() for _ in range(5)]

@@ -390,11 +390,502 @@ int launch_adj(sss_plan* p, const AdjArgs& a, int threads, size_t smem, int grid
     return SSS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Row-part adjoint.  The forward pass runs the row-part forward kernel and
+// keeps the state before every exponential (no recomputation); this kernel
+// then walks each trajectory backwards.  Per exponential it assembles Omega
+// on the row-part layout of the transposed pattern (rows of Omega^T are the
+// columns of Omega) and runs the transposed block series
+//     px <- (Omega^T px + G^T py)/j,   py <- mu + (Omega^T py)/j,  j = d..1,
+// from px = 0, py = mu: then py = E^T mu (the new adjoint) and
+// g = rho_before . px = mu^T L(Omega, G) rho_before.  Per entry three FMAs
+// (two chains share the gathered py value); G^T entries sit first in each
+// part so that only the first `ngx` positions carry the third FMA.  The x
+// channel's coefficients and derivative factors (cos, -a sin and segment at
+// every node) come from a ring filled kRing steps at a time, walking back.
+// Gradient sums are kept per node and segment in registers of lane 0 and
+// added to the output when the segment changes.
+struct AdjPartsArgs {
+    int M, K, Q, F, nch, nseg, ntraj, degree, T;
+    long n_steps;
+    double h, t0, dt;
+    int n_live, x_live, kc, ngx;
+    int live[kMaxG];
+    int gen_index[kMaxG];
+    const int* pcol;        // C*P*L transposed entry columns [e][l]
+    const unsigned* cw;     // kCloseMax*L close words [k][l]
+    const double* om0;      // K*C*P*L constant part of Omega^T per exponential
+    const double* gv;       // Ga*C*P*L transposed generator values [g][e][l]
+    const double* gx;       // C*P*L  x generator values (the G of the series)
+    const int* rbeg;        // L+1
+    const int* fwdpos;      // M: index of each row in the stored forward states
+    const double* rw;       // M
+    const double* tw;       // T
+    const double* toff;
+    const double* noff;
+    const double* W;
+    const double* states;   // ntraj*n_steps*K*M
+    const double* readout;  // ntraj*T
+    const double* prog;
+    double* J;
+    double* grad;
+    int* queue;
+    double inv_j[kAdjMaxTaylor + 1];
+};
+
+template <int L, int C, int P>
+__global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) {
+    extern __shared__ double smem[];
+    constexpr int CP = C * P;
+    const int M = a.M, NL = a.n_live, K = a.K, Q = a.Q, d = a.degree;
+    const int Ms = M + 2;  // rows, the zero row M, the sink row M+1
+    const int slot = threadIdx.x / L, li = threadIdx.x % L;
+    const size_t per_slot =
+        (6 * (size_t)Ms + 2 * (size_t)(L * C + 1) + (size_t)kRing * (Q * NL + K * NL + 3 * Q)) | 1;
+    double* sb = smem + slot * per_slot;
+    double* parts1 = sb + 6 * (size_t)Ms;
+    double* parts2 = parts1 + L * C + 1;
+    double* ringc = parts2 + L * C + 1;         // [s][k][live] node values
+    double* ring_ag = ringc + kRing * Q * NL;   // [s][e][live] CF weights
+    double* ring_d = ring_ag + kRing * K * NL;  // [s][k][3] cos, -a sin, segment of the x channel
+    double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
+    for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw[i];
+    for (int i = li; i < 6 * Ms; i += L) sb[i] = 0.0;
+    for (int i = li; i < 2 * (L * C + 1); i += L) parts1[i] = 0.0;
+    int col[CP];
+    double gx[CP];
+#pragma unroll
+    for (int e = 0; e < CP; e++) {
+        col[e] = __ldg(a.pcol + (size_t)e * L + li);
+        gx[e] = __ldg(a.gx + (size_t)e * L + li);
+    }
+    unsigned cw[kCloseMax];
+#pragma unroll
+    for (int k = 0; k < kCloseMax; k++) cw[k] = __ldg(a.cw + (size_t)k * L + li);
+    const int kc = a.kc, ngx = a.ngx;
+    const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
+    __syncthreads();
+
+    const unsigned lane_in_warp = threadIdx.x & 31;
+    const unsigned leader = lane_in_warp / L * L;
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    const double* zb = sb;    // stays zero
+    double* mu = sb + Ms;
+    double* yA = mu + Ms;
+    double* yB = yA + Ms;
+    double* xA = yB + Ms;
+    double* xB = xA + Ms;
+    double om[CP];
+
+    while (true) {
+        int nb = 0;
+        if (li == 0) nb = atomicAdd(a.queue, 1);
+        const int b = __shfl_sync(gmask, nb, leader);
+        if (b >= a.ntraj) break;
+        const double* prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
+        // objective from the forward readouts
+        {
+            double s = 0.0;
+            for (int t = li; t < a.T; t += L) s = fma(a.tw[t], a.readout[(size_t)b * a.T + t], s);
+#pragma unroll
+            for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+            if (li == 0) a.J[b] = s;
+        }
+        double* gb = a.grad + (size_t)b * a.nseg * 2;
+        // lane 0: running gradient sums per node, for segment cur_seg[k]
+        int cur_seg[kMaxQ];
+        double acc_a[kMaxQ], acc_p[kMaxQ];
+#pragma unroll
+        for (int k = 0; k < kMaxQ; k++) {
+            cur_seg[k] = -1;
+            acc_a[k] = 0.0;
+            acc_p[k] = 0.0;
+        }
+        for (int row = r0; row < r1; row++) mu[row] = 0.0;
+        __syncwarp(gmask);
+        const double* st_b = a.states + (size_t)b * a.n_steps * K * M;
+        int rp = kRing;
+        for (long n = a.n_steps - 1; n >= 0; n--) {
+            if ((n + 1) % a.F == 0) {
+                const double w = a.tw[(n + 1) / a.F - 1];
+                for (int row = r0; row < r1; row++) mu[row] = fma(w, s_rw[row], mu[row]);
+                __syncwarp(gmask);
+            }
+            if (rp == kRing) {
+                // steps n, n-1, ..., n-kRing+1: node values of the live channels;
+                // for the x channel also cos, -a sin and the segment
+                for (int i = li; i < kRing * Q * NL; i += L) {
+                    const int s = i / (Q * NL), rem = i - s * Q * NL, k = rem / NL, gi = rem - k * NL;
+                    const long ns = n - s;
+                    double val = 0.0, cs = 0.0, dph = 0.0;
+                    int sg = -1;
+                    if (ns >= 0) {
+                        const int ts = (int)(ns / a.F), rs = (int)(ns % a.F);
+                        const double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + rs)),
+                                                              __dmul_rn(a.dt, (double)ts)),
+                                                    __ldg(a.noff + k));
+                        const int g = a.gen_index[a.live[gi]];
+                        if (gi == a.x_live) {
+                            sg = x_segment(prog, a.nseg, tn);
+                            if (sg >= 0) {
+                                const double* q = prog + sg * 5;
+                                const double arg =
+                                    __dadd_rn(__dmul_rn(__dmul_rn(6.283185307179586, q[3]), tn), q[4]);
+                                cs = cos(arg);
+                                dph = -q[2] * sin(arg);
+                                val = q[2] == 0.0 ? q[1] : __dadd_rn(q[1], __dmul_rn(q[2], cs));
+                            }
+                        } else {
+                            val = (g - 1 < a.nch) ? channel_value(prog, a.nseg, g - 1, tn) : 0.0;
+                        }
+                    }
+                    ringc[i] = val;
+                    if (gi == a.x_live) {
+                        double* rd = ring_d + (s * Q + k) * 3;
+                        rd[0] = cs;
+                        rd[1] = dph;
+                        rd[2] = (double)sg;
+                    }
+                }
+                __syncwarp(gmask);
+                for (int i = li; i < kRing * K * NL; i += L) {
+                    const int s = i / (K * NL), rem = i - s * K * NL, e = rem / NL, gi = rem - e * NL;
+                    double w = 0.0;
+                    for (int k = 0; k < Q; k++)
+                        w = fma(__ldg(a.W + e * Q + k), ringc[(s * Q + k) * NL + gi], w);
+                    ring_ag[i] = w * a.h;
+                }
+                __syncwarp(gmask);
+                rp = 0;
+            }
+            for (int e_exp = 0; e_exp < K; e_exp++) {
+                const double* o0 = a.om0 + (size_t)e_exp * CP * L + li;
+#pragma unroll
+                for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
+                for (int gi = 0; gi < NL; gi++) {
+                    const double c = ring_ag[(rp * K + e_exp) * NL + gi];
+                    if (c == 0.0) continue;
+                    const double* gv = a.gv + (size_t)a.live[gi] * CP * L + li;
+#pragma unroll
+                    for (int e = 0; e < CP; e++) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);
+                }
+                const double* pxc = zb;
+                const double* pyc = mu;
+                double* pxn = xA;
+                double* pyn = yA;
+                for (int j = d; j >= 1; j--) {
+                    const double ij = a.inv_j[j];
+                    double s1[C], s2[C];
+#pragma unroll
+                    for (int c = 0; c < C; c++) {
+                        s1[c] = 0.0;
+                        s2[c] = 0.0;
+                    }
+#pragma unroll
+                    for (int q = 0; q < P; q++)
+#pragma unroll
+                        for (int c = 0; c < C; c++) {
+                            const int e = c * P + q;
+                            const double yv = pyc[col[e]];
+                            s2[c] = fma(om[e], yv, s2[c]);
+                            s1[c] = fma(om[e], pxc[col[e]], s1[c]);
+                            if (q < ngx) s1[c] = fma(gx[e], yv, s1[c]);
+                        }
+#pragma unroll
+                    for (int c = 0; c < C; c++) {
+                        parts1[li * C + c] = s1[c];
+                        parts2[li * C + c] = s2[c];
+                    }
+                    __syncwarp(gmask);
+                    double a1 = 0.0, a2 = 0.0;
+#pragma unroll
+                    for (int k = 0; k < kCloseMax; k++) {
+                        if (k >= kc) break;
+                        const unsigned w = cw[k];
+                        const int row = (int)(w & 0xffffu), pi = (int)((w >> 16) & 0x7fffu);
+                        const bool first = (w >> 31) != 0;
+                        a1 = fma(parts1[pi], ij, first ? 0.0 : a1);
+                        a2 = fma(parts2[pi], ij, first ? mu[row] : a2);
+                        pxn[row] = a1;
+                        pyn[row] = a2;
+                    }
+                    __syncwarp(gmask);
+                    pxc = pxn;
+                    pyc = pyn;
+                    pxn = (pxn == xA) ? xB : xA;
+                    pyn = (pyn == yA) ? yB : yA;
+                }
+                // g = rho_before . px;  mu <- E^T mu (the buffer holding it)
+                const double* rb = st_b + ((size_t)n * K + e_exp) * M;
+                double g = 0.0;
+                for (int row = r0; row < r1; row++) g = fma(rb[__ldg(a.fwdpos + row)], pxc[row], g);
+#pragma unroll
+                for (int o = L / 2; o > 0; o >>= 1) g += __shfl_xor_sync(gmask, g, o);
+                double* newmu = const_cast<double*>(pyc);
+                if (newmu == yA) yA = mu; else yB = mu;
+                mu = newmu;
+                if (li == 0) {
+#pragma unroll
+                    for (int k = 0; k < kMaxQ; k++) {
+                        if (k >= Q) break;
+                        const double* rd = ring_d + (rp * Q + k) * 3;
+                        const int sg = (int)rd[2];
+                        if (sg != cur_seg[k]) {
+                            if (cur_seg[k] >= 0) {
+                                gb[2 * cur_seg[k]] += acc_a[k];
+                                gb[2 * cur_seg[k] + 1] += acc_p[k];
+                            }
+                            cur_seg[k] = sg;
+                            acc_a[k] = 0.0;
+                            acc_p[k] = 0.0;
+                        }
+                        if (sg >= 0) {
+                            const double hw = a.h * __ldg(a.W + e_exp * Q + k);
+                            acc_a[k] = fma(hw * rd[0], g, acc_a[k]);
+                            acc_p[k] = fma(hw * rd[1], g, acc_p[k]);
+                        }
+                    }
+                }
+                __syncwarp(gmask);
+            }
+            rp++;
+        }
+        if (li == 0) {
+#pragma unroll
+            for (int k = 0; k < kMaxQ; k++)
+                if (k < Q && cur_seg[k] >= 0) {
+                    gb[2 * cur_seg[k]] += acc_a[k];
+                    gb[2 * cur_seg[k] + 1] += acc_p[k];
+                }
+        }
+        __syncwarp(gmask);
+    }
+}
+
+template <int L>
+int launch_adj_parts(sss_plan* p, int C, int P, const AdjPartsArgs& a, int threads, size_t smem,
+                     cudaStream_t st) {
+    auto go = [&](auto kern) -> int {
+        SSS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        SSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+        if (per_sm < 1) return fail(SSS_EINVAL, "adjoint kernel does not fit on an SM");
+        const int slots = threads / L;
+        const int grid = std::max(1, std::min((a.ntraj + slots - 1) / slots, per_sm * p->num_sms));
+        kern<<<grid, threads, smem, st>>>(a);
+        SSS_CUDA(cudaGetLastError());
+        return SSS_OK;
+    };
+    static_assert(sizeof(kPartShapes) / sizeof(kPartShapes[0]) == 4, "one case per part shape");
+    if (C == 1 && P == 4) return go(k_adjoint_parts<L, 1, 4>);
+    if (C == 2 && P == 4) return go(k_adjoint_parts<L, 2, 4>);
+    if (C == 4 && P == 4) return go(k_adjoint_parts<L, 4, 4>);
+    if (C == 2 && P == 8) return go(k_adjoint_parts<L, 2, 8>);
+    return fail(SSS_EINVAL, "no adjoint kernel for this part shape");
+}
+
+// Row-part adjoint: forward with stored states, then the backward kernel,
+// over trajectory chunks sized to the free device memory.  Returns
+// SSS_EINVAL (with nothing launched) when the pattern does not fit the
+// row-part kernels or the states of one trajectory do not fit in memory.
+int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+                      const double* d_prog, double t0, double dt, int T, int F,
+                      const double* h_rw, const double* h_tw, double* d_J, double* d_grad,
+                      cudaStream_t st) {
+    const int N = p->d.N, K = p->d.K, Q = p->d.Q;
+    BatchLayout Ly;
+    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {1}, true, &Ly, st, true))
+        return rc;
+    if (Ly.M == 0) return fail(SSS_EINVAL, "empty pattern");
+    if (Ly.substeps != 1) return fail(SSS_EINVAL, "the adjoint needs one sub-step per exponential");
+    if (Ly.degree > kAdjMaxTaylor) return fail(SSS_EINVAL, "Taylor degree too large for the adjoint");
+    int xg = -1;
+    for (int gi = 0; gi < Ly.Ga; gi++)
+        if (Ly.active[gi] == 1) xg = gi;
+    if (xg < 0) return fail(SSS_EINVAL, "the x generator is zero on the reachable rows");
+    const int M = Ly.M, Ga = Ly.Ga;
+    const long n_steps = (long)T * F;
+    const size_t per_traj = sizeof(double) * (size_t)n_steps * K * M;
+    size_t free_b = 0, total_b = 0;
+    SSS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = p->adj_max_bytes ? p->adj_max_bytes : free_b / 2;
+    if (per_traj > budget) return fail(SSS_EINVAL, "adjoint states of one trajectory exceed memory");
+    const int chunk = (int)std::min<size_t>((size_t)ntraj, budget / per_traj);
+
+    // ---- backward layout: the transposed pattern, x-generator entries first ----
+    std::vector<int> rows_reached(M);
+    for (int i = 0; i < M; i++) rows_reached[i] = Ly.row_orig[Ly.newpos[i]];
+    const SparseGenerators& sp = p->sparse;
+    std::vector<std::vector<BatchLayout::Ent>> rowsT(M);
+    std::vector<std::vector<char>> prioT(M);
+    for (int i = 0; i < M; i++)
+        for (const BatchLayout::Ent& en : Ly.row_ents[i]) {
+            rowsT[en.col].push_back({i, en.q});
+            prioT[en.col].push_back(sp.val[(size_t)1 * sp.nnz + en.q] != 0.0);
+        }
+    BatchLayout TL;
+    const int Lb = ntraj <= 8 * p->num_sms ? 32 : 16;
+    const int threads = 32;
+    int ngx = 0;
+    if (int rc = parts_layout_rows(p, rowsT, prioT, Lb, threads, 3, 2, Ly.active, rows_reached, &TL, &ngx))
+        return rc;
+    const int CP = TL.C * TL.P;
+
+    // ---- forward tables (x channel kept live) ----
+    PartsForward fw;
+    if (int rc = parts_forward_prepare(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {1}, p->w_adjf, &fw, st))
+        return rc;
+
+    // ---- backward tables ----
+    const double h = dt / F;
+    std::vector<int> live;
+    std::vector<double> om0((size_t)K * CP * Lb, 0.0);
+    for (int gi = 0; gi < Ga; gi++) {
+        const int g = Ly.active[gi];
+        if (g != 0 && (g == 1 || !Ly.chan_const[g])) {
+            live.push_back(gi);
+            continue;
+        }
+        const double X = g == 0 ? 1.0 : Ly.chan_value[g];
+        for (int e = 0; e < K; e++) {
+            double s = 0.0;
+            for (int k = 0; k < Q; k++) s = std::fma(p->W[e * Q + k], X, s);
+            const double ag = s * h;
+            for (int i = 0; i < CP * Lb; i++) {
+                double& o = om0[(size_t)e * CP * Lb + i];
+                o = std::fma(ag, TL.gv[(size_t)gi * CP * Lb + i], o);
+            }
+        }
+    }
+    int x_live = -1;
+    for (size_t i = 0; i < live.size(); i++)
+        if (live[i] == xg) x_live = (int)i;
+    std::vector<double> rwb(M, 0.0), tw(h_tw, h_tw + T), toff(F), noff(Q);
+    for (int k = 0; k < M; k++) rwb[k] = h_rw ? h_rw[TL.row_orig[k]] : 0.0;
+    for (int r = 0; r < F; r++) toff[r] = ((double)r * dt) / F;
+    for (int k = 0; k < Q; k++) noff[k] = (dt * p->nodes[k]) / F;
+    std::vector<int> fwdpos(M), rbeg(Lb + 1, 0);
+    for (int i = 0; i < M; i++) fwdpos[TL.newpos[i]] = Ly.newpos[i];
+    for (int l = 0; l < Lb; l++) rbeg[l + 1] = rbeg[l] + (int)TL.lane_of[l].size();
+    // blob: gv | gx | om0 | rw | tw | toff | noff | pcol | cw | rbeg | fwdpos
+    std::vector<double> dbl(TL.gv);
+    const size_t o_gx = dbl.size();
+    dbl.insert(dbl.end(), TL.gv.begin() + (size_t)xg * CP * Lb, TL.gv.begin() + (size_t)(xg + 1) * CP * Lb);
+    const size_t o_om0 = dbl.size();
+    dbl.insert(dbl.end(), om0.begin(), om0.end());
+    const size_t o_rw = dbl.size();
+    dbl.insert(dbl.end(), rwb.begin(), rwb.end());
+    const size_t o_tw = dbl.size();
+    dbl.insert(dbl.end(), tw.begin(), tw.end());
+    const size_t o_toff = dbl.size();
+    dbl.insert(dbl.end(), toff.begin(), toff.end());
+    const size_t o_noff = dbl.size();
+    dbl.insert(dbl.end(), noff.begin(), noff.end());
+    std::vector<int> ints(TL.pcol);
+    const size_t o_cw = ints.size();
+    ints.insert(ints.end(), TL.cw.begin(), TL.cw.end());
+    const size_t o_rbeg = ints.size();
+    ints.insert(ints.end(), rbeg.begin(), rbeg.end());
+    const size_t o_fwd = ints.size();
+    ints.insert(ints.end(), fwdpos.begin(), fwdpos.end());
+    const size_t bytes = sizeof(double) * dbl.size() + sizeof(int) * ints.size();
+    if (int rc = p->w_adjb.ensure(bytes + 64)) return rc;
+    {
+        std::vector<char> blob(bytes);
+        memcpy(blob.data(), dbl.data(), sizeof(double) * dbl.size());
+        memcpy(blob.data() + sizeof(double) * dbl.size(), ints.data(), sizeof(int) * ints.size());
+        SSS_CUDA(cudaMemcpyAsync(p->w_adjb.p, blob.data(), bytes, cudaMemcpyHostToDevice, st));
+        SSS_CUDA(cudaStreamSynchronize(st));  // the host blob goes out of scope
+    }
+    const double* dv = p->w_adjb.as<double>();
+    const int* di = reinterpret_cast<const int*>(dv + dbl.size());
+
+    AdjPartsArgs a{};
+    a.M = M; a.K = K; a.Q = Q; a.F = F; a.nch = nch; a.nseg = nseg; a.degree = Ly.degree; a.T = T;
+    a.n_steps = n_steps; a.h = h; a.t0 = t0; a.dt = dt;
+    a.n_live = (int)live.size();
+    a.x_live = x_live;
+    a.kc = TL.kc;
+    a.ngx = ngx;
+    for (size_t i = 0; i < live.size(); i++) a.live[i] = live[i];
+    for (int gi = 0; gi < Ga; gi++) a.gen_index[gi] = Ly.active[gi];
+    a.gv = dv;
+    a.gx = dv + o_gx;
+    a.om0 = dv + o_om0;
+    a.rw = dv + o_rw;
+    a.tw = dv + o_tw;
+    a.toff = dv + o_toff;
+    a.noff = dv + o_noff;
+    a.pcol = di;
+    a.cw = reinterpret_cast<const unsigned*>(di + o_cw);
+    a.rbeg = di + o_rbeg;
+    a.fwdpos = di + o_fwd;
+    a.W = p->d_gens.as<double>() + p->gens.size();
+    for (int j = 0; j <= kAdjMaxTaylor; j++) a.inv_j[j] = j ? 1.0 / j : 0.0;
+    const size_t smem = sizeof(double) *
+        (((6 * (size_t)(M + 2) + 2 * (size_t)(Lb * TL.C + 1) +
+           (size_t)kRing * (Q * live.size() + K * live.size() + 3 * Q)) | 1) * (threads / Lb) + M);
+    if (smem > 227 * 1024) return fail(SSS_EINVAL, "adjoint kernel: shared memory per CTA too large");
+
+    // ---- buffers and chunks ----
+    if (int rc = p->w_states.ensure(per_traj * chunk)) return rc;
+    if (int rc = p->w_adjro.ensure(sizeof(double) * (size_t)chunk * T)) return rc;
+    if (int rc = p->w_adjst.ensure(sizeof(double) * (size_t)chunk * N)) return rc;
+    if (int rc = p->w_queue.ensure(sizeof(int) * 4)) return rc;
+    SSS_CUDA(cudaMemsetAsync(d_J, 0, sizeof(double) * ntraj, st));
+    SSS_CUDA(cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ntraj * nseg * 2, st));
+    if (!p->ev_begin) {
+        SSS_CUDA(cudaEventCreate(&p->ev_begin));
+        SSS_CUDA(cudaEventCreate(&p->ev_end));
+    }
+    SSS_CUDA(cudaEventRecord(p->ev_begin, st));
+    int launches = 0;
+    for (int b0 = 0; b0 < ntraj; b0 += chunk) {
+        const int nb = std::min(chunk, ntraj - b0);
+        double* state = p->w_adjst.as<double>();
+        const double* prog = d_prog + (size_t)b0 * nch * nseg * 5;
+        SSS_CUDA(cudaMemcpyAsync(state, d_rho0 + (size_t)b0 * N, sizeof(double) * (size_t)nb * N,
+                                 cudaMemcpyDeviceToDevice, st));
+        if (int rc = parts_forward_launch(p, fw, nb, state, prog, t0, T, p->w_adjro.as<double>(),
+                                          p->w_states.as<double>(), st))
+            return rc;
+        AdjPartsArgs ab = a;
+        ab.ntraj = nb;
+        ab.states = p->w_states.as<double>();
+        ab.readout = p->w_adjro.as<double>();
+        ab.prog = prog;
+        ab.J = d_J + b0;
+        ab.grad = d_grad + (size_t)b0 * nseg * 2;
+        ab.queue = p->w_queue.as<int>();
+        SSS_CUDA(cudaMemsetAsync(ab.queue, 0, sizeof(int), st));
+        int rc = Lb == 32 ? launch_adj_parts<32>(p, TL.C, TL.P, ab, threads, smem, st)
+                          : launch_adj_parts<16>(p, TL.C, TL.P, ab, threads, smem, st);
+        if (rc) return rc;
+        launches += 2;
+    }
+    SSS_CUDA(cudaEventRecord(p->ev_end, st));
+    p->ev_recorded = true;
+    p->last_launches = launches;
+    p->last_batch_lanes = Lb;
+    p->last_degree = Ly.degree;
+    p->last_substeps = 1;
+    p->last_rows = M;
+    p->last_nnz = (int)Ly.nnz;
+    p->last_variant = 4;
+    return SSS_OK;
+}
+
 }  // namespace
 
 int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 const double* d_prog, double t0, double dt, int T, int F, const double* h_rw,
                 const double* h_tw, double* d_J, double* d_grad, cudaStream_t st) {
+    if (p->batch_variant == 0 || p->batch_variant == 4) {
+        const int rc = adjoint_run_parts(p, ntraj, d_rho0, nch, nseg, d_prog, t0, dt, T, F, h_rw,
+                                         h_tw, d_J, d_grad, st);
+        if (rc != SSS_EINVAL || p->batch_variant == 4) return rc;
+        set_error("");
+    }
     const int N = p->d.N, K = p->d.K, Q = p->d.Q;
     if (p->d.G < 2) return fail(SSS_EINVAL, "the adjoint needs the x generator (G >= 2)");
     BatchLayout Ly;

@@ -437,6 +437,12 @@ int sss_plan_set_batch_config(sss_plan* p, int lanes, int cta_threads, int varia
     return SSS_OK;
 }
 
+int sss_plan_set_adjoint_memory(sss_plan* p, size_t max_bytes) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    p->adj_max_bytes = max_bytes;
+    return SSS_OK;
+}
+
 int sss_plan_batch_info(const sss_plan* p, int* lanes, int* degree, int* substeps, int* rows,
                         int* nnz, double* kernel_ms) {
     if (!p) return fail(SSS_EINVAL, "null plan");
@@ -463,7 +469,8 @@ void sss_plan_destroy(sss_plan* p) {
                       &p->d_sp_rowptr, &p->d_sp_col, &p->d_sp_val, &p->d_row_map,
                       &p->w_prop, &p->w_in, &p->w_out, &p->w_prog, &p->w_tab, &p->w_aux,
                       &p->w_queue, &p->w_ro, &p->w_fin, &p->w_samples, &p->w_status,
-                      &p->w_state};
+                      &p->w_state, &p->w_adjf, &p->w_adjb, &p->w_states, &p->w_adjro,
+                      &p->w_adjst};
     for (DevBuf* b : bufs) b->release();
     if (p->ev_begin) cudaEventDestroy(p->ev_begin);
     if (p->ev_end) cudaEventDestroy(p->ev_end);

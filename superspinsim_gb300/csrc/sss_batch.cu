@@ -81,10 +81,6 @@ int build_sparse(sss_plan* p) {
 namespace {
 
 constexpr int kMaxTaylor = 24;
-constexpr int kCloseMax = 8;   // close slots per lane in the row-part variant
-constexpr int kRing = 16;      // fine steps of coefficients per refill (row-part variant)
-// (C parts per lane, P entries per part) shapes of the row-part kernel
-constexpr int kPartShapes[][2] = {{1, 4}, {2, 4}, {4, 4}, {2, 8}};
 
 struct BatchArgs {
     int M;        // state rows kept (reachable)
@@ -117,6 +113,8 @@ struct BatchArgs {
     int kc;                    // close slots per lane (max over lanes)
     int n_live;                // generators assembled per step (the others are in om0)
     int live[kMaxG];           // their active-generator slots
+    double* states;            // state before every exponential, or null:
+    long st_steps;             //   [((b*st_steps + n)*K + e)*M + row], n = step since t_begin
     double inv_j[kMaxTaylor + 1];
 };
 
@@ -626,6 +624,11 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             rp = 0;
         }
         for (int e_exp = K - 1; e_exp >= 0; e_exp--) {
+            if (a.states) {
+                double* sp = a.states +
+                             (((size_t)b * a.st_steps + (size_t)(t - a.t_begin) * a.F + r) * K + e_exp) * M;
+                for (int row = r0; row < r1; row++) sp[row] = v[row];
+            }
             const double* o0 = a.om0 + (size_t)e_exp * CP * L + li;
 #pragma unroll
             for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
@@ -781,28 +784,34 @@ static void choose_taylor(double beta, int forced_degree, int* degree, int* subs
     *substeps = best_m;
 }
 
-// Row-part layout (k_batch_parts): rows cut into parts of at most P
-// entries, parts spread over the L*C lane slots, rows given to owner lanes
-// by longest-processing-time first on their close cost (one slot per part,
-// one for an empty row).  Picks the (C, P) shape with the fewest FP64
-// instructions per Horner term (C*P + kc), then the shortest dependent
-// chain (P + kc).
-static int layout_parts(sss_plan* p, int degree, int substeps, int L, int M, int Ga, long nnz,
-                        const std::vector<int>& rows_reached, BatchLayout* out) {
+// Row-part layout of a row pattern `rows` (per reachable row: compressed
+// column and SparseGenerators index of each entry): rows cut into parts of
+// at most P entries, parts spread over the L*C lane slots (part j -> lane
+// j % L, chain j / L), rows given to owner lanes by longest-processing-time
+// first on their close cost (one slot per part, one for an empty row).
+// Picks the (C, P) shape minimising w_chain*C*P + w_close*kc (FP64
+// instructions per Horner term), then the shortest chain P + kc.  Entries
+// flagged in `prio` (may be empty) are spread evenly over their row's parts
+// and placed first in each part; `nprio` returns the most flagged entries
+// in any part.  Fills newpos/row_orig (owner order), lane_of, pcol, cw, gv
+// (for `active`), entry_q, C, P, kc, L, E = C*P, threads.
+int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows,
+                      const std::vector<std::vector<char>>& prio, int L, int threads, int w_chain,
+                      int w_close, const std::vector<int>& active,
+                      const std::vector<int>& rows_reached, BatchLayout* out, int* nprio) {
     BatchLayout& Ly = *out;
     const SparseGenerators& sp = p->sparse;
-    const std::vector<std::vector<BatchLayout::Ent>>& row_ents = Ly.row_ents;
+    const int M = (int)rows.size(), Ga = (int)active.size();
     if (L != 8 && L != 16 && L != 32)
         return fail(SSS_EINVAL, "row-part variant needs 8, 16 or 32 lanes per trajectory");
-    const int threads = p->batch_threads > 0 ? p->batch_threads : 64;
     if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
-    auto nparts = [&](int i, int P) { return ((int)row_ents[i].size() + P - 1) / P; };
+    auto nparts = [&](int i, int P) { return ((int)rows[i].size() + P - 1) / P; };
     // owners by LPT on close cost; returns kc
     auto owners = [&](int P, std::vector<std::vector<int>>* own) {
         std::vector<int> order(M);
         std::iota(order.begin(), order.end(), 0);
         auto cost = [&](int i) { return std::max(1, nparts(i, P)); };
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
         std::vector<int> load(L, 0);
         own->assign(L, {});
         for (int i : order) {
@@ -811,7 +820,7 @@ static int layout_parts(sss_plan* p, int degree, int substeps, int L, int M, int
             (*own)[l].push_back(i);
         }
         for (auto& o : *own) std::sort(o.begin(), o.end());
-        return *std::max_element(load.begin(), load.end());
+        return M ? *std::max_element(load.begin(), load.end()) : 0;
     };
     int bC = 0, bP = 0, bkc = 0;
     long best_cost = -1, best_path = 0;
@@ -823,7 +832,7 @@ static int layout_parts(sss_plan* p, int degree, int substeps, int L, int M, int
         std::vector<std::vector<int>> own;
         const int kc = owners(P, &own);
         if (kc > kCloseMax) continue;
-        const long cost = C * P + kc, path = P + kc;
+        const long cost = (long)w_chain * C * P + (long)w_close * kc, path = P + kc;
         if (best_cost < 0 || cost < best_cost || (cost == best_cost && path < best_path)) {
             best_cost = cost; best_path = path; bC = C; bP = P; bkc = kc;
         }
@@ -844,33 +853,51 @@ static int layout_parts(sss_plan* p, int degree, int substeps, int L, int M, int
         for (int l = 0; l < L; l++)
             for (int i : own[l]) { newpos[i] = k; row_orig[k] = rows_reached[i]; k++; }
     }
-    // parts in row order, part j -> lane j % L, chain j / L
     Ly.pcol.assign((size_t)CP * L, M);
+    Ly.entry_q.assign((size_t)CP * L, -1);
     Ly.gv.assign((size_t)Ga * CP * L, 0.0);
     std::vector<std::vector<int>> part_slots(M);  // per row: smem slot lane*C + c of each part
+    int most = 0;
     {
         int j = 0;
         for (int i = 0; i < M; i++) {
-            const auto& ents = row_ents[i];
+            const auto& ents = rows[i];
             const int n = (int)ents.size(), np = nparts(i, P);
-            int at = 0;
-            for (int q = 0; q < np; q++) {
-                const int len = n / np + (q < n % np ? 1 : 0);
+            if (np == 0) continue;
+            // entries of each part: flagged entries dealt round-robin first,
+            // then the others fill up to the part sizes
+            std::vector<int> size(np), order_f, order_o;
+            for (int q = 0; q < np; q++) size[q] = n / np + (q < n % np ? 1 : 0);
+            for (int e = 0; e < n; e++)
+                (!prio.empty() && prio[i][e] ? order_f : order_o).push_back(e);
+            std::vector<std::vector<int>> pe(np);
+            int q = 0;
+            for (int e : order_f) {
+                for (int tries = 0; (int)pe[q].size() >= size[q] && tries < np; tries++) q = (q + 1) % np;
+                pe[q].push_back(e);
+                q = (q + 1) % np;
+            }
+            for (int qq = 0; qq < np; qq++) most = std::max(most, (int)pe[qq].size());
+            size_t oi = 0;
+            for (int qq = 0; qq < np; qq++)
+                while ((int)pe[qq].size() < size[qq]) pe[qq].push_back(order_o[oi++]);
+            for (int qq = 0; qq < np; qq++) {
                 const int lane = j % L, c = j / L;
-                for (int e = 0; e < len; e++) {
-                    const BatchLayout::Ent& en = ents[at + e];
+                for (int e = 0; e < (int)pe[qq].size(); e++) {
+                    const BatchLayout::Ent& en = ents[pe[qq][e]];
                     const size_t idx = (size_t)(c * P + e) * L + lane;
                     Ly.pcol[idx] = newpos[en.col];
+                    Ly.entry_q[idx] = en.q;
                     for (int gi = 0; gi < Ga; gi++)
                         Ly.gv[((size_t)gi * CP + c * P + e) * L + lane] =
-                            sp.val[(size_t)Ly.active[gi] * sp.nnz + en.q];
+                            sp.val[(size_t)active[gi] * sp.nnz + en.q];
                 }
-                at += len;
                 part_slots[i].push_back(lane * C + c);
                 j++;
             }
         }
     }
+    if (nprio) *nprio = most;
     const unsigned zero_part = (unsigned)(L * C) << 16, first = 1u << 31;
     Ly.cw.assign((size_t)kCloseMax * L, (unsigned)(M + 1) | zero_part | first);
     for (int l = 0; l < L; l++) {
@@ -895,16 +922,13 @@ static int layout_parts(sss_plan* p, int degree, int substeps, int L, int M, int
     Ly.E = CP;
     Ly.use_reg = false;
     Ly.epl = 0;
-    Ly.nnz = nnz;
-    Ly.degree = degree;
-    Ly.substeps = substeps;
     Ly.threads = threads;
     return SSS_OK;
 }
 
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
-                 bool allow_register, BatchLayout* out, cudaStream_t st) {
+                 bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts) {
     const int N = p->d.N, G = p->d.G;
     BatchLayout& Ly = *out;
     const SparseGenerators& sp = p->sparse;
@@ -1033,9 +1057,24 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
         while (L < cap && (long)ntraj * L < want) L *= 2;
     }
     if (p->batch_lanes > 0) L = p->batch_lanes;
-    if (allow_register && p->batch_variant == 4)
-        return layout_parts(p, degree, substeps, p->batch_lanes > 0 ? L : std::max(L, 8), M, Ga,
-                            nnz, rows_reached, out);
+    // row-part kernel: asked for (4), or automatic (0) when the pattern fits.
+    // Automatic lanes: 32 (one trajectory per warp, the shortest chains)
+    // while the batch gives at most two warps per SM sub-partition, else 16
+    // (two trajectories per warp, fewer instructions per trajectory)
+    if (force_parts || (allow_register && (p->batch_variant == 4 || p->batch_variant == 0))) {
+        const int Lp = p->batch_lanes > 0 && !force_parts
+                           ? L
+                           : ((long)ntraj <= 8L * p->num_sms ? 32 : 16);
+        const int rc = parts_layout_rows(p, Ly.row_ents, {}, Lp,
+                                         p->batch_threads > 0 ? p->batch_threads : 32, 1, 1, active,
+                                         rows_reached, out, nullptr);
+        if (rc == SSS_OK) {
+            Ly.nnz = nnz;
+            Ly.degree = degree;
+            Ly.substeps = substeps;
+        }
+        if (rc == SSS_OK || p->batch_variant == 4 || force_parts) return rc;
+    }
     // ---- rows to lanes, balanced by entry count.  The register variant
     // pads each row to an even length (two chains); an empty row carries
     // zero entries so that it still closes ----
@@ -1121,28 +1160,17 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
     return SSS_OK;
 }
 
-int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
-                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st) {
-    const int N = p->d.N;
-    p->batch_ready = false;
-    p->batch_empty = false;
-    BatchLayout Ly;
-    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st)) return rc;
-    if (Ly.M == 0) {
-        p->batch_ready = true;
-        p->batch_empty = true;
-        p->batch_ntraj = ntraj;
-        p->batch_nch = nch;
-        p->batch_nseg = nseg;
-        p->batch_dt = dt;
-        p->batch_F = F;
-        return SSS_OK;
-    }
-    const int M = Ly.M, Ga = Ly.Ga, L = Ly.L, E = Ly.E, epl = Ly.epl, degree = Ly.degree,
+// Device tables (into `tables`) and kernel arguments of a batch layout;
+// `keep_live` generators are never folded into the row-part kernel's
+// constant part of Omega.
+static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int nseg, double dt,
+                     int F, const double* h_rw, const std::vector<int>& keep_live, DevBuf& tables,
+                     BatchArgs* out, size_t* smem, cudaStream_t st) {
+    const int M = Ly.M, Ga = Ly.Ga, L = Ly.L, E = Ly.E, degree = Ly.degree,
               substeps = Ly.substeps, threads = Ly.threads;
     const bool use_reg = Ly.use_reg;
     const bool one_chain = p->batch_variant == 3;
-    const long nnz = Ly.nnz;
+    const int N = p->d.N;
     const std::vector<int>& active = Ly.active;
     const std::vector<int>& row_orig = Ly.row_orig;
     std::vector<double> rw(M, 0.0);
@@ -1170,7 +1198,8 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
         std::vector<double> om0((size_t)p->d.K * CP * L, 0.0);
         for (int gi = 0; gi < Ga; gi++) {
             const int g = active[gi];
-            if (g != 0 && !Ly.chan_const[g]) {
+            const bool keep = std::find(keep_live.begin(), keep_live.end(), g) != keep_live.end();
+            if (g != 0 && (!Ly.chan_const[g] || keep)) {
                 live.push_back(gi);
                 continue;
             }
@@ -1202,16 +1231,16 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
         }
     }
     size_t bytes = sizeof(double) * dbl.size() + sizeof(unsigned) * words.size() + sizeof(int) * ints.size();
-    if (int rc = p->d_sp_val.ensure(bytes + 64)) return rc;
+    if (int rc = tables.ensure(bytes + 64)) return rc;
     std::vector<char> blob(bytes);
     memcpy(blob.data(), dbl.data(), sizeof(double) * dbl.size());
     memcpy(blob.data() + sizeof(double) * dbl.size(), words.data(), sizeof(unsigned) * words.size());
     memcpy(blob.data() + sizeof(double) * dbl.size() + sizeof(unsigned) * words.size(), ints.data(),
            sizeof(int) * ints.size());
-    SSS_CUDA(cudaMemcpyAsync(p->d_sp_val.p, blob.data(), bytes, cudaMemcpyHostToDevice, st));
+    SSS_CUDA(cudaMemcpyAsync(tables.p, blob.data(), bytes, cudaMemcpyHostToDevice, st));
     if (int rc = p->w_queue.ensure(sizeof(int) * 4)) return rc;
     SSS_CUDA(cudaMemsetAsync(p->w_queue.p, 0, sizeof(int) * 4, st));
-    const double* dv = p->d_sp_val.as<double>();
+    const double* dv = tables.as<double>();
     const unsigned* dw = reinterpret_cast<const unsigned*>(dv + dbl.size());
     const int* di = reinterpret_cast<const int*>(dw + words.size());
 
@@ -1243,8 +1272,54 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     a.queue = p->w_queue.as<int>();
     for (int j = 0; j <= kMaxTaylor; j++) a.inv_j[j] = j ? 1.0 / j : 0.0;
 
+    *out = a;
+    if (Ly.parts) {
+        const size_t per_slot = (3 * (size_t)(M + 2) + L * Ly.C + 1 +
+                                 (size_t)kRing * (p->d.Q + p->d.K) * live.size()) | 1;
+        *smem = sizeof(double) * ((threads / L) * per_slot + M);
+    } else if (use_reg) {
+        const size_t per_slot = ((one_chain ? 4 : 5) * (size_t)M + kMaxQ * kMaxG) | 1;
+        *smem = sizeof(double) * ((threads / L) * per_slot + M);
+    } else {
+        const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
+        const size_t per_slot = ((size_t)E * L + 3 * M + kMaxQ * kMaxG) | 1;
+        *smem = sizeof(double) * (shared_words + (threads / L) * per_slot);
+    }
+    if (*smem > 227 * 1024)
+        return fail(SSS_EINVAL, "batched kernel needs " + std::to_string(*smem) +
+                                    " bytes of shared memory per CTA (max 232448); use fewer "
+                                    "threads per CTA");
+    return SSS_OK;
+}
+
+int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
+                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st) {
+    p->batch_ready = false;
+    p->batch_empty = false;
+    BatchLayout Ly;
+    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st)) return rc;
+    if (Ly.M == 0) {
+        p->batch_ready = true;
+        p->batch_empty = true;
+        p->batch_ntraj = ntraj;
+        p->batch_nch = nch;
+        p->batch_nseg = nseg;
+        p->batch_dt = dt;
+        p->batch_F = F;
+        return SSS_OK;
+    }
+    BatchArgs a{};
+    size_t smem = 0;
+    if (int rc = make_args(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {}, p->d_sp_val, &a, &smem, st))
+        return rc;
     static_assert(sizeof(BatchArgs) <= sizeof(p->batch_args), "BatchArgs does not fit the plan");
     memcpy(p->batch_args, &a, sizeof(BatchArgs));
+    p->batch_smem = smem;
+    const int M = Ly.M, Ga = Ly.Ga, L = Ly.L, E = Ly.E, epl = Ly.epl, degree = Ly.degree,
+              substeps = Ly.substeps, threads = Ly.threads;
+    const bool use_reg = Ly.use_reg;
+    const bool one_chain = p->batch_variant == 3;
+    const long nnz = Ly.nnz;
     p->batch_use_reg = use_reg;
     p->batch_one_chain = one_chain;
     p->batch_parts = Ly.parts;
@@ -1259,22 +1334,6 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     p->batch_dt = dt;
     p->batch_F = F;
     p->batch_has_rw = h_rw != nullptr;
-    if (Ly.parts) {
-        const size_t per_slot = (3 * (size_t)(M + 2) + L * Ly.C + 1 +
-                                 (size_t)kRing * (p->d.Q + p->d.K) * live.size()) | 1;
-        p->batch_smem = sizeof(double) * ((threads / L) * per_slot + M);
-    } else if (use_reg) {
-        const size_t per_slot = ((one_chain ? 4 : 5) * (size_t)M + kMaxQ * kMaxG) | 1;
-        p->batch_smem = sizeof(double) * ((threads / L) * per_slot + M);
-    } else {
-        const size_t shared_words = (size_t)Ga * E * L + M + ((size_t)E * L + L + 1) / 2;
-        const size_t per_slot = ((size_t)E * L + 3 * M + kMaxQ * kMaxG) | 1;
-        p->batch_smem = sizeof(double) * (shared_words + (threads / L) * per_slot);
-    }
-    if (p->batch_smem > 227 * 1024)
-        return fail(SSS_EINVAL, "batched kernel needs " + std::to_string(p->batch_smem) +
-                                    " bytes of shared memory per CTA (max 232448); use fewer "
-                                    "threads per CTA");
     p->last_batch_lanes = L;
     p->last_degree = degree;
     p->last_substeps = substeps;
@@ -1343,6 +1402,51 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
     }
     p->last_launches = rc == SSS_OK ? 1 : 0;
     return rc;
+}
+
+int parts_forward_prepare(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int nseg,
+                          double dt, int F, const double* h_rw, const std::vector<int>& keep_live,
+                          DevBuf& tables, PartsForward* fw, cudaStream_t st) {
+    if (!Ly.parts) return fail(SSS_EINVAL, "not a row-part layout");
+    BatchArgs a{};
+    size_t smem = 0;
+    if (int rc = make_args(p, Ly, ntraj, nch, nseg, dt, F, h_rw, keep_live, tables, &a, &smem, st))
+        return rc;
+    static_assert(sizeof(BatchArgs) <= sizeof(fw->args), "BatchArgs does not fit");
+    memcpy(fw->args, &a, sizeof(BatchArgs));
+    fw->smem = smem;
+    fw->L = Ly.L;
+    fw->C = Ly.C;
+    fw->P = Ly.P;
+    fw->threads = Ly.threads;
+    return SSS_OK;
+}
+
+int parts_forward_launch(sss_plan* p, const PartsForward& fw, int ntraj, double* d_state,
+                         const double* d_prog, double t0, int T, double* d_readout,
+                         double* d_states, cudaStream_t st) {
+    BatchArgs a;
+    memcpy(&a, fw.args, sizeof(BatchArgs));
+    a.ntraj = ntraj;
+    a.rho0 = d_state;
+    a.fin = d_state;
+    a.prog = d_prog;
+    a.samples = nullptr;
+    a.readout = d_readout;
+    a.rw = d_readout ? a.rw : nullptr;
+    a.trace = nullptr;
+    a.t0 = t0;
+    a.t_begin = 0;
+    a.t_end = T;
+    a.T_max = T;
+    a.states = d_states;
+    a.st_steps = (long)T * a.F;
+    SSS_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int), st));
+    switch (fw.L) {
+        case 8: return launch_parts<8>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
+        case 16: return launch_parts<16>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
+        default: return launch_parts<32>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
+    }
 }
 
 int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,

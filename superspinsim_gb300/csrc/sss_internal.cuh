@@ -15,6 +15,11 @@ constexpr int kMaxQ = 3;      // Gauss-Legendre nodes
 constexpr int kMaxK = 6;      // exponentials per step
 constexpr int kMaxCh = 4;     // coefficient channels
 constexpr int kPlainMaxN = 52;  // dense shared-memory propagator path
+// row-part kernels (forward and adjoint)
+constexpr int kCloseMax = 8;    // close slots per lane
+constexpr int kRing = 16;       // fine steps of coefficients per refill
+// (C parts per lane, P entries per part) shapes instantiated
+constexpr int kPartShapes[][2] = {{1, 4}, {2, 4}, {4, 4}, {2, 8}};
 
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
@@ -109,6 +114,10 @@ struct sss_plan {
     double batch_dt = 0.0;
     size_t batch_smem = 0;
     sss::DevBuf w_state;
+    // adjoint (row-part path): forward and backward tables, stored states,
+    // readouts, state buffer
+    sss::DevBuf w_adjf, w_adjb, w_states, w_adjro, w_adjst;
+    size_t adj_max_bytes = 0;  // stored-state memory of the adjoint, 0: half the free memory
 };
 
 namespace sss {
@@ -133,5 +142,28 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
                  cudaStream_t st, double* d_trace = nullptr);
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
-                 bool allow_register, BatchLayout* out, cudaStream_t st);
+                 bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts = false);
+int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows,
+                      const std::vector<std::vector<char>>& prio, int L, int threads, int w_chain,
+                      int w_close, const std::vector<int>& active,
+                      const std::vector<int>& rows_reached, BatchLayout* out, int* nprio);
+// Row-part forward kernel prepared outside the plan's batch state (for the
+// adjoint): opaque kernel arguments and launch shape.
+struct PartsForward {
+    alignas(16) unsigned char args[1024];
+    size_t smem = 0;
+    int L = 0, C = 0, P = 0, threads = 0;
+};
+// Build the device tables of a row-part layout into `tables` and the
+// forward kernel's arguments.  Generators in `keep_live` are never folded
+// into the constant part of Omega.
+int parts_forward_prepare(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int nseg,
+                          double dt, int F, const double* h_rw, const std::vector<int>& keep_live,
+                          DevBuf& tables, PartsForward* fw, cudaStream_t st);
+// Launch it on `ntraj` trajectories (state in place, programs, readout
+// (ntraj x T) or null, and optionally the state before every exponential:
+// states[((b*T*F + n)*K + e)*M + row], rows in the layout's order).
+int parts_forward_launch(sss_plan* p, const PartsForward& fw, int ntraj, double* d_state,
+                         const double* d_prog, double t0, int T, double* d_readout,
+                         double* d_states, cudaStream_t st);
 }  // namespace sss

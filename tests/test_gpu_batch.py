@@ -27,8 +27,9 @@ def _excited_weights(vmap):
 
 
 @pytest.mark.parametrize("name", ["nv7_n49", "nv7_n19"])
-@pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 2), (8, 2),
-                                           (0, 3), (32, 3), (0, 4), (8, 4), (16, 4), (32, 4)])
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 1), (16, 1),
+                                           (0, 2), (8, 2), (0, 3), (32, 3), (0, 4), (8, 4),
+                                           (16, 4), (32, 4)])
 def test_batch_odmr_against_oracle(name, lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
