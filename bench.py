@@ -49,7 +49,7 @@ LASER = 10/65.9
 METRIC = "NV-7 ODMR traj-steps/s"
 # DRAM bytes (read + write) of one batched-kernel launch on this workload,
 # from ncu (profiles/batch_odmr_nv7.md)
-TRAFFIC_BYTES = 592896
+TRAFFIC_BYTES = 880896
 
 
 def nv7_model():

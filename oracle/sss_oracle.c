@@ -31,7 +31,7 @@
  * Coefficients come from a segment program evaluated with libm cos (the
  * same function the reference's samplers call through math.cos).
  *
- * Parity pinned: tests/golden/*.npz hold outputs of the reference itself.
+ * Parity pinned: the .npz fixtures under tests/golden hold outputs of the reference itself.
  */
 #include <math.h>
 #include <stdlib.h>
