@@ -184,6 +184,33 @@ int sss_adjoint_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                     const double* time_weights, double* J, double* grad,
                     int host, void* cuda_stream);
 
+/* Equivalence-class ("kernel") mode.  The plan's generators act on the
+ * r = N dimensional image of the orthonormal basis P (n_full x N, row-major),
+ * the complement of the generators' common kernel.  sss_simulate and
+ * sss_simulate_device then take and return states of n_full entries:
+ * rho(t) = rho0 + P (U_r(t) - I) P^T rho0, i.e. the full propagator
+ * P U_r P^T + (I - P P^T), with the common-kernel components held fixed.
+ * Replaces the reference's equivalence-class sandwich and kernel addition
+ * (generate_simulator.py:1789-1797, 2043-2071), whose residual sandwich reads
+ * out of bounds (:1047); this is the form it intends.  n_full = 0 clears the
+ * mode.  Batched runs and the adjoint reject projected plans. */
+int sss_plan_set_projection(sss_plan* plan, int n_full, const double* image_projection);
+
+/* Unitary mode.  The plan's N = 2n generators are real forms of n x n
+ * complex matrices (entry (i, j) at [2i][2j] real and [2i+1][2j] imaginary,
+ * generate_generators.py:2725-2746), so the integrator propagates an
+ * operator U.  sss_simulate then returns densities conj(U) rho0 U^T -- what
+ * the reference's Kronecker product, unitary copy and elimination /
+ * duplication sandwich produce (generate_simulator.py:1394-1504, 2074-2101),
+ * without its out-of-bounds reads (:1026) -- flattened by `map` (nd rows
+ * y, x, c as the vectorisation map; rho0 is read the same way, off-diagonal
+ * rows mirrored to their Hermitian partner) or, with map = NULL, all 2n^2
+ * entries row-major.  With the reference's generators (the real form of
+ * +iH) this is the unitary evolution of the Liouvillian mode whenever H is
+ * real.  n = 0 clears the mode.  Batched runs and the adjoint reject
+ * unitary plans. */
+int sss_plan_set_unitary(sss_plan* plan, int n, int nd, const int* map);
+
 /* Kernel launches issued by the last sss_simulate / sss_batch_run call on
  * this plan (for launch accounting). */
 int sss_plan_last_launches(const sss_plan* plan);

@@ -24,6 +24,7 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
 SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
            "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
+           "sss_plan_set_projection", "sss_plan_set_unitary",
            "sss_fp64_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
            "sss_batch_launch", "sss_last_error",
            "sss_plan_destroy"]
@@ -76,6 +77,10 @@ def load(build_if_missing=True):
         L.sss_plan_set_batch_config.argtypes = [vp, i, i, i]
         L.sss_plan_set_adjoint_memory.argtypes = [vp, ctypes.c_size_t]
         L.sss_plan_set_adjoint_memory.restype = i
+        L.sss_plan_set_projection.argtypes = [vp, i, dp]
+        L.sss_plan_set_projection.restype = i
+        L.sss_plan_set_unitary.argtypes = [vp, i, i, ctypes.POINTER(ctypes.c_int)]
+        L.sss_plan_set_unitary.restype = i
         L.sss_plan_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, dp]
         L.sss_fp64_peak.argtypes = [dp, vp]
         L.sss_adjoint_run.argtypes = [vp, i, vp, i, i, vp, d, d, i, i, dp, dp, vp, vp, i, vp]
@@ -139,6 +144,7 @@ class Plan:
             gens = np.ascontiguousarray(generators, dtype=np.float64)
             G, N, _ = gens.shape
         self.N, self.G, self.K, self.Q = N, G, K, Q
+        self.n_state = N   # entries of a state in and of a sample out of simulate
         desc = PlanDesc(N, G, K, Q, flags, expm, quartic_repeats, taylor_degree)
         h = ctypes.c_void_p()
         check(L.sss_plan_create(ctypes.byref(h), ctypes.byref(desc), dptr(gens),
@@ -162,12 +168,45 @@ class Plan:
     def handle(self):
         return self._h
 
+    def set_projection(self, image_projection):
+        """Equivalence-class mode: generators act on the image of P
+        (n_full x N); simulate then takes and returns n_full-entry states.
+        None clears it."""
+        if image_projection is None:
+            check(load().sss_plan_set_projection(self._h, 0, None))
+            self.n_state = self.N
+            return
+        P = np.ascontiguousarray(image_projection, dtype=np.float64)
+        check(load().sss_plan_set_projection(self._h, P.shape[0], dptr(P)))
+        self.n_state = P.shape[0]
+
+    def set_unitary(self, n, vectorisation_map=None):
+        """Unitary mode for an n-level system (N = 2n operator generators);
+        simulate then takes and returns densities flattened by the map (or
+        all 2n^2 entries row-major).  n = 0 clears it."""
+        if not n:
+            check(load().sss_plan_set_unitary(self._h, 0, 0, None))
+            self.n_state = self.N
+            return
+        if vectorisation_map is None:
+            check(load().sss_plan_set_unitary(self._h, int(n), 0, None))
+            self.n_state = 2*n*n
+            return
+        vm = np.ascontiguousarray(vectorisation_map, dtype=np.int32).reshape(-1, 3)
+        check(load().sss_plan_set_unitary(self._h, int(n), vm.shape[0],
+                                          vm.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        self.n_state = vm.shape[0]
+
     def simulate(self, rho0, programs, t0, dt, T, F, table=None, stream=None):
-        """rho0 (B, N); programs (B, nch, nseg, 5) or None with table
-        (B, F*T*Q, G).  Returns (B, T, N)."""
+        """rho0 (B, n_state); programs (B, nch, nseg, 5) or None with table
+        (B, F*T*Q, G).  Returns (B, T, n_state) (n_state = N unless a
+        projection or unitary mode is set)."""
         rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
         B = rho0.shape[0]
-        out = np.empty((B, T, self.N))
+        if rho0.shape[1] != self.n_state:
+            raise ValueError(f"rho0 has {rho0.shape[1]} entries per state, the plan takes "
+                             f"{self.n_state}")
+        out = np.empty((B, T, self.n_state))
         if programs is not None:
             programs = np.ascontiguousarray(programs, dtype=np.float64)
             nch, nseg = programs.shape[1], programs.shape[2]

@@ -151,6 +151,47 @@ int sss_plan_set_rotating(sss_plan* p, const double* gn, const double* dlast, in
     return SSS_OK;
 }
 
+int sss_plan_set_projection(sss_plan* p, int n_full, const double* P) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (p->u_n) return fail(SSS_EINVAL, "a unitary-mode plan cannot take a projection");
+    if (n_full == 0) {
+        p->n_full = 0;
+        return SSS_OK;
+    }
+    const int N = p->d.N;
+    if (n_full < N || !P) return fail(SSS_EINVAL, "projection needs n_full >= N and P (n_full x N)");
+    if (!finite_all(P, (size_t)n_full * N)) return fail(SSS_ENONFINITE, "projection contains NaN or Inf");
+    if (int rc = upload(p->d_P, P, (size_t)n_full * N)) return rc;
+    p->n_full = n_full;
+    return SSS_OK;
+}
+
+int sss_plan_set_unitary(sss_plan* p, int n, int nd, const int* map) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (p->n_full) return fail(SSS_EINVAL, "a projected plan cannot run in unitary mode");
+    if (n == 0) {
+        p->u_n = 0;
+        return SSS_OK;
+    }
+    if (n < 1 || 2 * n != p->d.N) return fail(SSS_EINVAL, "unitary mode needs N = 2n");
+    if (map) {
+        if (nd < 1 || nd > 2 * n * n) return fail(SSS_EINVAL, "bad vectorisation map size");
+        for (int i = 0; i < nd; i++) {
+            const int y = map[3 * i], x = map[3 * i + 1], c = map[3 * i + 2];
+            if (y < 0 || y >= n || x < 0 || x >= n || c < 0 || c > 1)
+                return fail(SSS_EINVAL, "vectorisation map entry out of range");
+        }
+        std::vector<double> m(map, map + 3 * (size_t)nd);  // stored as doubles
+        if (int rc = upload(p->d_umap, m.data(), m.size())) return rc;
+    } else {
+        nd = 2 * n * n;
+    }
+    p->u_n = n;
+    p->u_nd = nd;
+    p->u_mapped = map != nullptr;
+    return SSS_OK;
+}
+
 static int check_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
                      const double* programs, const double* tab, double dt, int T, int F,
                      const void* out) {
@@ -173,7 +214,7 @@ static int simulate_impl(sss_plan* p, int ntraj, const double* rho0, int nch, in
     p->last_launches = 0;
     if (ntraj == 0 || T == 0) return SSS_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    const int N = p->d.N;
+    const int N = p->state_in();  // entries of a state in and of a sample out
     const double *d_rho0 = rho0, *d_prog = programs, *d_tab = tab;
     double* d_out = out;
     if (host) {
@@ -235,6 +276,8 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
         return rc;
     if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
     if (p->rotating) return fail(SSS_EINVAL, "batched runs support the lab frame only");
+    if (p->n_full || p->u_n)
+        return fail(SSS_EINVAL, "batched runs support neither projected nor unitary plans");
     if (readout && !readout_weights) return fail(SSS_EINVAL, "readout needs readout_weights");
     p->last_launches = 0;
     if (ntraj == 0 || T_max == 0) return SSS_OK;
@@ -324,6 +367,8 @@ int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nse
     if (!programs || !readout_weights || !time_weights || !grad)
         return fail(SSS_EINVAL, "the adjoint needs programs, readout and time weights, and grad");
     if (p->rotating) return fail(SSS_EINVAL, "the adjoint supports the lab frame only");
+    if (p->n_full || p->u_n)
+        return fail(SSS_EINVAL, "the adjoint supports neither projected nor unitary plans");
     p->last_launches = 0;
     if (ntraj == 0 || T == 0) return SSS_OK;
     cudaStream_t st = (cudaStream_t)stream;
@@ -364,6 +409,8 @@ int sss_batch_prepare(sss_plan* p, int ntraj, const double* rho0, int nch, int n
     if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, 1, F, rho0)) return rc;
     if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
     if (p->rotating) return fail(SSS_EINVAL, "batched runs support the lab frame only");
+    if (p->n_full || p->u_n)
+        return fail(SSS_EINVAL, "batched runs support neither projected nor unitary plans");
     if (ntraj == 0) return fail(SSS_EINVAL, "empty batch");
     return batch_prepare(p, ntraj, rho0, nch, nseg, programs, dt, F, readout_weights,
                          (cudaStream_t)stream);

@@ -118,6 +118,17 @@ struct sss_plan {
     // readouts, state buffer
     sss::DevBuf w_adjf, w_adjb, w_states, w_adjro, w_adjst;
     size_t adj_max_bytes = 0;  // stored-state memory of the adjoint, 0: half the free memory
+    // equivalence-class (kernel) mode: states of n_full entries, image basis P
+    // (n_full x N); unitary mode: operator generators of a u_n-level system
+    // (N = 2 u_n), densities of u_nd entries (map u_map rows y, x, c, or all
+    // 2 u_n^2 entries row-major)
+    int n_full = 0;
+    sss::DevBuf d_P;
+    int u_n = 0, u_nd = 0;
+    bool u_mapped = false;
+    sss::DevBuf d_umap;
+    // entries of one input state and of one output sample of sss_simulate
+    int state_in() const { return n_full ? n_full : (u_n ? u_nd : d.N); }
 };
 
 namespace sss {

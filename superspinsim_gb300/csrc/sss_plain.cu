@@ -262,27 +262,45 @@ k_step_propagators(PlainArgs a) {
     for (int idx = threadIdx.x; idx < NN; idx += blockDim.x) dst[idx] = TE[idx];
 }
 
-// v <- v + S v (residual) or S v, for t = 0..T-1; writes out[b][t] (lab basis)
+// v <- v + S v (residual) or S v, for t = 0..T-1; writes out[b][t] (lab basis).
+// With an image basis P (n_full x N, equivalence-class mode): the chain runs
+// on x0 = P^T rho0 and the output is rho0 + P (y - x0), y the chain's lab-basis
+// vector -- the full propagator P (I + E) P^T + (I - P P^T): components in the
+// generators' common kernel stay fixed (the intended form of the reference's
+// sandwich and kernel addition, generate_simulator.py:2043-2071).
+// state[b] holds the running vector between chunks (in the eigenbasis when
+// rotating), followed by x0 when projecting.
 __global__ void __launch_bounds__(kPlainThreads)
 k_chain(const double* __restrict__ S, const double* __restrict__ rho0, const double* __restrict__ V,
-        const double* __restrict__ Vinv, int N, int T, int residual, int t_begin,
-        double* __restrict__ state, double* __restrict__ out) {
-    __shared__ double v[kPlainMaxN], w[kPlainMaxN];
+        const double* __restrict__ Vinv, const double* __restrict__ P, int n_full, int N, int T,
+        int residual, int t_begin, double* __restrict__ state, double* __restrict__ out) {
+    __shared__ double v[kPlainMaxN], w[kPlainMaxN], x0[kPlainMaxN], y[kPlainMaxN];
     const int b = blockIdx.x, NN = N * N;
-    // state[b] holds the chain's running vector between chunks (in the
-    // eigenbasis when rotating)
+    const int nio = P ? n_full : N;  // entries of a state in and of a sample out
+    const int sw = P ? 2 * N : N;    // state words per trajectory
     if (t_begin == 0) {
         if (threadIdx.x < N) {
             double acc = 0.0;
-            if (Vinv) {
-                for (int k = 0; k < N; k++) acc = fma(Vinv[threadIdx.x * N + k], rho0[(size_t)b * N + k], acc);
+            if (P) {
+                for (int k = 0; k < n_full; k++)
+                    acc = fma(P[(size_t)k * N + threadIdx.x], rho0[(size_t)b * nio + k], acc);
             } else {
                 acc = rho0[(size_t)b * N + threadIdx.x];
+            }
+            x0[threadIdx.x] = acc;
+        }
+        __syncthreads();
+        if (threadIdx.x < N) {
+            double acc = x0[threadIdx.x];
+            if (Vinv) {
+                acc = 0.0;
+                for (int k = 0; k < N; k++) acc = fma(Vinv[threadIdx.x * N + k], x0[k], acc);
             }
             v[threadIdx.x] = acc;
         }
     } else if (threadIdx.x < N) {
-        v[threadIdx.x] = state[(size_t)b * N + threadIdx.x];
+        v[threadIdx.x] = state[(size_t)b * sw + threadIdx.x];
+        if (P) x0[threadIdx.x] = state[(size_t)b * sw + N + threadIdx.x];
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -304,10 +322,142 @@ k_chain(const double* __restrict__ S, const double* __restrict__ rho0, const dou
                 o = 0.0;
                 for (int k = 0; k < N; k++) o = fma(V[threadIdx.x * N + k], v[k], o);
             }
-            out[(size_t)(t_begin + t) * N + threadIdx.x] = o;
+            y[threadIdx.x] = o;
+        }
+        __syncthreads();
+        double* ot = out + (size_t)(t_begin + t) * nio;
+        if (!P) {
+            if (threadIdx.x < N) ot[threadIdx.x] = y[threadIdx.x];
+        } else {
+            for (int i = threadIdx.x; i < n_full; i += blockDim.x) {
+                double acc = rho0[(size_t)b * nio + i];
+                for (int k = 0; k < N; k++) acc = fma(P[(size_t)i * N + k], y[k] - x0[k], acc);
+                ot[i] = acc;
+            }
         }
     }
-    if (threadIdx.x < N) state[(size_t)b * N + threadIdx.x] = v[threadIdx.x];
+    if (threadIdx.x < N) {
+        state[(size_t)b * sw + threadIdx.x] = v[threadIdx.x];
+        if (P) state[(size_t)b * sw + N + threadIdx.x] = x0[threadIdx.x];
+    }
+}
+
+// Unitary mode (generate_simulator.py:2074-2101 with :1394-1504): the step
+// propagators act on a u_n-level operator in real 2n x 2n form (entry (i, j)
+// of the complex matrix at [2i][2j] real, [2i+1][2j] imaginary).  One CTA per
+// trajectory keeps the running operator propagator M (M - I in residual
+// form; in the eigenbasis when rotating, U = V M V^-1), and after every
+// sample writes the density conj(U) rho0 U^T -- what the reference's
+// Kronecker product, unitary copy and elimination/duplication sandwich give
+// -- in the basis of the vectorisation map (rows y, x, c as doubles), or all
+// 2n^2 entries row-major.  state[b] holds M between chunks.
+__global__ void __launch_bounds__(kPlainThreads)
+k_chain_unitary(const double* __restrict__ S, const double* __restrict__ rho0,
+                const double* __restrict__ V, const double* __restrict__ Vinv,
+                const double* __restrict__ umap, int n, int nd, int T, int residual, int t_begin,
+                double* __restrict__ state, double* __restrict__ out) {
+    extern __shared__ double sm[];
+    const int D = 2 * n, DD = D * D, nn = n * n;
+    double* M = sm;           // D x D
+    double* A = M + DD;       // D x D scratch
+    double* U = A + DD;       // D x D lab-basis propagator
+    double* r0 = U + DD;      // n x n complex rho0 (re, im interleaved)
+    double* tm = r0 + 2 * nn; // n x n complex conj(U) rho0
+    const int b = blockIdx.x;
+    auto map_row = [&](int i, int* y, int* x, int* c) {
+        if (umap) {
+            *y = (int)umap[3 * i];
+            *x = (int)umap[3 * i + 1];
+            *c = (int)umap[3 * i + 2];
+        } else {
+            *y = (i >> 1) / n;
+            *x = (i >> 1) % n;
+            *c = i & 1;
+        }
+    };
+    for (int i = threadIdx.x; i < 2 * nn; i += blockDim.x) r0[i] = 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // rho0 from its flattened form; mapped off-diagonal entries mirror
+        // to the Hermitian partner
+        for (int i = 0; i < nd; i++) {
+            int y, x, c;
+            map_row(i, &y, &x, &c);
+            const double val = rho0[(size_t)b * nd + i];
+            r0[2 * (y * n + x) + c] = val;
+            if (umap && y != x) r0[2 * (x * n + y) + c] = c ? -val : val;
+        }
+    }
+    for (int i = threadIdx.x; i < DD; i += blockDim.x)
+        M[i] = t_begin == 0 ? ((!residual && i / D == i % D) ? 1.0 : 0.0) : state[(size_t)b * DD + i];
+    __syncthreads();
+    for (int t = 0; t < T; t++) {
+        const double* Et = S + ((size_t)b * T + t) * DD;
+        // M <- (I + E) M - I = E + M + E M (residual), or E M
+        for (int idx = threadIdx.x; idx < DD; idx += blockDim.x) {
+            const int i = idx / D, j = idx - i * D;
+            double acc = residual ? __ldg(Et + idx) + M[idx] : 0.0;
+            for (int k = 0; k < D; k++) acc = fma(__ldg(Et + i * D + k), M[k * D + j], acc);
+            A[idx] = acc;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < DD; idx += blockDim.x) M[idx] = A[idx];
+        __syncthreads();
+        // U (lab basis) = V (I + M) V^-1, or I + M
+        if (V) {
+            for (int idx = threadIdx.x; idx < DD; idx += blockDim.x) {
+                const int i = idx / D, j = idx - i * D;
+                double acc = residual ? Vinv[idx] : 0.0;
+                for (int k = 0; k < D; k++) acc = fma(M[i * D + k], Vinv[k * D + j], acc);
+                A[idx] = acc;
+            }
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < DD; idx += blockDim.x) {
+                const int i = idx / D, j = idx - i * D;
+                double acc = 0.0;
+                for (int k = 0; k < D; k++) acc = fma(V[i * D + k], A[k * D + j], acc);
+                U[idx] = acc;
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < DD; idx += blockDim.x)
+                U[idx] = M[idx] + ((residual && idx / D == idx % D) ? 1.0 : 0.0);
+        }
+        __syncthreads();
+        // tm = conj(Uc) rho0, Uc[i][k] = U[2i][2k] + i U[2i+1][2k]
+        for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
+            const int i = idx / n, j = idx - i * n;
+            double re = 0.0, im = 0.0;
+            for (int k = 0; k < n; k++) {
+                const double ur = U[(2 * i) * D + 2 * k], ui = -U[(2 * i + 1) * D + 2 * k];
+                const double rr = r0[2 * (k * n + j)], ri = r0[2 * (k * n + j) + 1];
+                re = fma(ur, rr, re);
+                re = fma(-ui, ri, re);
+                im = fma(ur, ri, im);
+                im = fma(ui, rr, im);
+            }
+            tm[2 * idx] = re;
+            tm[2 * idx + 1] = im;
+        }
+        __syncthreads();
+        // rho = tm Uc^T: rho[y][x] = sum_k tm[y][k] Uc[x][k]; write the mapped entries
+        double* ot = out + (size_t)(t_begin + t) * nd;
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+            int y, x, c;
+            map_row(i, &y, &x, &c);
+            double re = 0.0, im = 0.0;
+            for (int k = 0; k < n; k++) {
+                const double ur = U[(2 * x) * D + 2 * k], ui = U[(2 * x + 1) * D + 2 * k];
+                const double tr = tm[2 * (y * n + k)], ti = tm[2 * (y * n + k) + 1];
+                re = fma(tr, ur, re);
+                re = fma(-ti, ui, re);
+                im = fma(tr, ui, im);
+                im = fma(ti, ur, im);
+            }
+            ot[i] = c ? im : re;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < DD; i += blockDim.x) state[(size_t)b * DD + i] = M[i];
 }
 
 }  // namespace
@@ -323,7 +473,12 @@ int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
     size_t per_sample = NN * sizeof(double);
     int chunk = (int)std::min<size_t>((size_t)T, std::max<size_t>(1, (2ull << 30) / per_sample));
     if (int rc = p->w_prop.ensure(per_sample * (size_t)chunk)) return rc;
-    if (int rc = p->w_aux.ensure(sizeof(double) * (size_t)N)) return rc;
+    const int nio = p->state_in();  // entries of a state in and of a sample out
+    if (int rc = p->w_aux.ensure(sizeof(double) * (p->u_n ? NN : 2 * (size_t)N))) return rc;
+    const size_t usmem = sizeof(double) * (3 * NN + 4 * (size_t)p->u_n * p->u_n);
+    if (p->u_n)
+        SSS_CUDA(cudaFuncSetAttribute(k_chain_unitary, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)usmem));
     size_t smem = 8 * NN * sizeof(double);
     SSS_CUDA(cudaFuncSetAttribute(k_step_propagators, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
@@ -363,9 +518,16 @@ int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
             SSS_CUDA(cudaGetLastError());
             const double* V = p->rotating ? p->d_V.as<double>() : nullptr;
             const double* Vi = p->rotating ? p->d_Vinv.as<double>() : nullptr;
-            k_chain<<<1, kPlainThreads, 0, st>>>(p->w_prop.as<double>(), d_rho0 + (size_t)b * N, V, Vi,
-                                                 N, Tc, a.residual ? 1 : 0, t_begin,
-                                                 p->w_aux.as<double>(), d_out + (size_t)b * T * N);
+            if (p->u_n)
+                k_chain_unitary<<<1, kPlainThreads, usmem, st>>>(
+                    p->w_prop.as<double>(), d_rho0 + (size_t)b * nio, V, Vi,
+                    p->u_mapped ? p->d_umap.as<double>() : nullptr, p->u_n, p->u_nd, Tc,
+                    a.residual ? 1 : 0, t_begin, p->w_aux.as<double>(), d_out + (size_t)b * T * nio);
+            else
+                k_chain<<<1, kPlainThreads, 0, st>>>(
+                    p->w_prop.as<double>(), d_rho0 + (size_t)b * nio, V, Vi,
+                    p->n_full ? p->d_P.as<double>() : nullptr, p->n_full, N, Tc,
+                    a.residual ? 1 : 0, t_begin, p->w_aux.as<double>(), d_out + (size_t)b * T * nio);
             launches++;
             SSS_CUDA(cudaGetLastError());
         }
@@ -501,7 +663,7 @@ extern "C" int sss_simulate_noalloc(const sss_plan_desc* d, const double* genera
         a.out = props;
         k_step_propagators<<<dim3(Tc, 1), kPlainThreads, smem, st>>>(a);
         SSS_CUDA(cudaGetLastError());
-        k_chain<<<1, kPlainThreads, 0, st>>>(props, rho0, nullptr, nullptr, N, Tc,
+        k_chain<<<1, kPlainThreads, 0, st>>>(props, rho0, nullptr, nullptr, nullptr, 0, N, Tc,
                                              a.residual ? 1 : 0, t_begin, chain_state, out);
         SSS_CUDA(cudaGetLastError());
     }
