@@ -161,35 +161,20 @@ def rotating_tables(generators_rotating, doubles, singles, nodes, dt, F,
     return out, np.ascontiguousarray(df[-1]), np.ascontiguousarray(sf[-1])
 
 
-def simulate(generators, rho0, t0, tf, dt, programs, *, K, W, nodes, F,
-             R=35, residual=True, vectorisation_map=None, rotating=None,
-             mode="reference", degree=12, threads=0, flat_out=False):
-    """Run the oracle for one or more trajectories.
-
-    generators: (G, N, N) lab-frame generators (when ``rotating`` is given,
-        the rotating-frame generators from ``make_rotating`` go in
-        ``rotating["generators_rotating"]`` and this argument is unused).
-    rho0: (n, n) complex, or (B, n, n) for B trajectories.
-    programs: (4, S, 5) coefficient program, or (B, 4, S, 5).
-    rotating: dict with generators_rotating, vectors_real,
-        inv_vectors_real, doubles, singles (reference make_rotating output).
-    mode: "reference" (the reference's algorithm) or "vector".
-    Returns (time (T,), density (T, n, n) or (B, T, n, n) complex).
-    """
+def simulate_flat(generators, flat0, t0, tf, dt, programs, *, K, W, nodes, F,
+                  R=35, residual=True, rotating=None, mode="reference", degree=12,
+                  threads=0):
+    """The oracle on flattened states: flat0 (B, N) in the lab basis,
+    programs (B, 4, S, 5).  Returns (time (T,), states (B, T, N)), lab
+    basis."""
     W = np.ascontiguousarray(W, dtype=np.float64)
     nodes = np.ascontiguousarray(nodes, dtype=np.float64)
     Kw, Q = W.shape
     assert Kw == K
-    single = np.asarray(rho0).ndim == 2
-    rho0 = np.asarray(rho0)
+    flat0 = np.asarray(flat0, dtype=np.float64)
     programs = np.asarray(programs, dtype=np.float64)
-    if single:
-        rho0 = rho0[None]
-        programs = programs[None]
-    B = rho0.shape[0]
-    n = rho0.shape[1]
+    B = flat0.shape[0]
     T = number_of_samples(t0, tf, dt)
-    vmap = vectorisation_map
     if rotating is not None:
         gens, dlast, slast = rotating_tables(
             rotating["generators_rotating"], rotating["doubles"],
@@ -206,7 +191,6 @@ def simulate(generators, rho0, t0, tf, dt, programs, *, K, W, nodes, F,
         dlast = slast = V = Vi = None
         D = S = 0
     gens = np.ascontiguousarray(gens)
-    flat0 = np.stack([flatten(r, vmap, N) for r in rho0])
     if rotating is not None and mode == "vector":
         flat0 = flat0 @ Vi.T
     flat0 = np.ascontiguousarray(flat0)
@@ -223,12 +207,75 @@ def simulate(generators, rho0, t0, tf, dt, programs, *, K, W, nodes, F,
         raise RuntimeError(f"oracle failed with status {status}")
     if rotating is not None and mode == "vector":
         out = out @ V.T
-    time = t0 + dt*(np.arange(T) + 1)
-    if flat_out:
-        res = out
+    return t0 + dt*(np.arange(T) + 1), out
+
+
+def simulate(generators, rho0, t0, tf, dt, programs, *, K, W, nodes, F,
+             R=35, residual=True, vectorisation_map=None, rotating=None,
+             mode="reference", degree=12, threads=0, flat_out=False):
+    """Run the oracle for one or more trajectories.
+
+    generators: (G, N, N) lab-frame generators (when ``rotating`` is given,
+        the rotating-frame generators from ``make_rotating`` go in
+        ``rotating["generators_rotating"]`` and this argument is unused).
+    rho0: (n, n) complex, or (B, n, n) for B trajectories.
+    programs: (4, S, 5) coefficient program, or (B, 4, S, 5).
+    rotating: dict with generators_rotating, vectors_real,
+        inv_vectors_real, doubles, singles (reference make_rotating output).
+    mode: "reference" (the reference's algorithm) or "vector".
+    Returns (time (T,), density (T, n, n) or (B, T, n, n) complex).
+    """
+    single = np.asarray(rho0).ndim == 2
+    rho0 = np.asarray(rho0)
+    programs = np.asarray(programs, dtype=np.float64)
+    if single:
+        rho0 = rho0[None]
+        programs = programs[None]
+    n = rho0.shape[1]
+    if rotating is not None:
+        N = np.asarray(rotating["generators_rotating"]).shape[-1]
     else:
-        res = unflatten(out, vmap, n)
+        N = np.asarray(generators).shape[1]
+    flat0 = np.stack([flatten(r, vectorisation_map, N) for r in rho0])
+    time, out = simulate_flat(generators, flat0, t0, tf, dt, programs, K=K, W=W,
+                              nodes=nodes, F=F, R=R, residual=residual,
+                              rotating=rotating, mode=mode, degree=degree,
+                              threads=threads)
+    res = out if flat_out else unflatten(out, vectorisation_map, n)
     return time, (res[0] if single else res)
+
+
+def simulate_kernel(generators_image, image_projection, rho0, t0, tf, dt,
+                    programs, *, vectorisation_map, rotating=None, **kw):
+    """Equivalence-class mode as the reference intends it
+    (generate_simulator.py:2043-2071): the generators act on the image of P
+    (n_full x r) and the common-kernel components stay fixed, rho(t) = rho0 +
+    P (U_r(t) - I) P^T rho0.  rho0 (n, n); returns (time, density (T, n, n))."""
+    P = np.asarray(image_projection, dtype=np.float64)
+    flat = flatten(np.asarray(rho0), vectorisation_map, P.shape[0])
+    x0 = P.T @ flat
+    time, out = simulate_flat(generators_image, x0[None], t0, tf, dt,
+                              np.asarray(programs)[None], rotating=rotating, **kw)
+    full = flat[None] + (out[0] - x0[None]) @ P.T
+    return time, unflatten(full, vectorisation_map, np.asarray(rho0).shape[0])
+
+
+def simulate_unitary(generators, rho0, t0, tf, dt, programs, *,
+                     vectorisation_map, rotating=None, **kw):
+    """Unitary mode as the reference's pipeline intends it
+    (generate_simulator.py:2074-2101, Kronecker product :1394-1425): the
+    real 2n x 2n generators propagate the operator U column by column, and
+    the density is conj(U) rho0 U^T.  rho0 (n, n); returns (time, density
+    (T, n, n)); ``vectorisation_map`` is not needed (full matrices)."""
+    rho0 = np.asarray(rho0, dtype=complex)
+    n = rho0.shape[0]
+    cols = np.zeros((n, 2*n))
+    for j in range(n):
+        cols[j, 2*j] = 1.0
+    progs = np.repeat(np.asarray(programs)[None], n, axis=0)
+    time, out = simulate_flat(generators, cols, t0, tf, dt, progs, rotating=rotating, **kw)
+    U = np.transpose(out[:, :, 0::2] + 1j*out[:, :, 1::2], (1, 2, 0))  # (T, n, n)
+    return time, np.conj(U) @ rho0 @ np.transpose(U, (0, 2, 1))
 
 
 def max_threads():

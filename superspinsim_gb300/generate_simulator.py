@@ -19,11 +19,20 @@ Coefficients: ``sampler`` is either a ``superspinsim_gb300.program.Program``
 ``sampler(time, row)`` writing the G coefficients; a callable is sampled on
 the host at every node time into a table that is uploaded with the run.
 
+Equivalence-class mode (``use_kernel`` with ``image_projection`` P): the
+generators act on the image of P and the states keep their full size; the
+device lifts the result, rho(t) = rho0 + P (U_r - I) P^T rho0 (the form the
+reference's sandwich and kernel addition intend, :1789-1797, :2043-2071).
+Unitary mode (``use_unitary``): the generators are real 2n x 2n operator
+forms and the device returns conj(U) rho0 U^T, what the reference's
+Kronecker product and elimination/duplication sandwich give (:2074-2101);
+the elimination and duplication matrices are accepted but not needed.
+
 Differences from the reference, all raising instead of silently changing
 behaviour: ``use_cuda=False`` (there is no CPU path), a ``datatype`` other
-than float64, and the equivalence-class (``use_kernel``) and unitary
-(``use_unitary``) modes raise ``NotImplementedError``; ``use_cayley`` raises
-``TypeError`` as the reference's ``raise "..."`` does (:53-54).
+than float64, kernel and unitary modes together, and either mode beyond the
+dense path's size; ``use_cayley`` raises ``TypeError`` as the reference's
+``raise "..."`` does (:53-54).
 
 ``expm`` selects the exponential: ``"taylor"`` (default; degree-12 Taylor
 polynomial after norm-chosen scaling, accurate to rounding) or
@@ -160,10 +169,8 @@ def generate_simulator(
         raise NotImplementedError("only float64 is supported")
     if use_cayley:
         raise TypeError("Cayley not implemented")
-    if use_kernel:
-        raise NotImplementedError("equivalence-class (use_kernel) mode is not implemented")
-    if use_unitary:
-        raise NotImplementedError("unitary (use_unitary) mode is not implemented")
+    if use_kernel and use_unitary:
+        raise NotImplementedError("kernel and unitary modes together are not supported")
     if expm not in ("taylor", "reference"):
         raise ValueError("expm must be 'taylor' or 'reference'")
     generators = np.ascontiguousarray(generators, dtype=np.float64)
@@ -171,19 +178,40 @@ def generate_simulator(
     if use_hermitian and vectorisation_map is None:
         use_hermitian = False
     vmap = np.asarray(vectorisation_map) if use_hermitian else None
-    if vmap is not None and vmap.shape[0] != N:
-        raise ValueError("vectorisation_map rows must equal the generator size")
+    projection = None
+    if use_kernel:
+        if image_projection is None:
+            raise ValueError("use_kernel needs image_projection")
+        projection = np.ascontiguousarray(image_projection, dtype=np.float64)
+        if projection.ndim != 2 or projection.shape[1] != N:
+            raise ValueError("image_projection must be (full size, generator size)")
+        Ns = projection.shape[0]          # entries of a flattened density
+    elif use_unitary:
+        if N % 2:
+            raise ValueError("unitary generators must have an even size (2n)")
+        Ns = vmap.shape[0] if vmap is not None else 2*(N//2)**2
+    else:
+        Ns = N
+    if vmap is not None and vmap.shape[0] != Ns:
+        raise ValueError("vectorisation_map rows must equal the state size")
     W, nodes = method(number_of_exponentials)
     F = int(number_of_fine_divisions)
     expm_code = _lib.SSS_EXPM_TAYLOR if expm == "taylor" else _lib.SSS_EXPM_REFERENCE
     state = {"plan": None, "h": None}
 
+    def with_mode(plan):
+        if projection is not None:
+            plan.set_projection(projection)
+        elif use_unitary:
+            plan.set_unitary(N//2, vmap)
+        return plan
+
     def plan_for(fine_step):
         if not use_rotating:
             if state["plan"] is None:
-                state["plan"] = _lib.Plan(generators, W, nodes, residual=use_residual,
-                                          expm=expm_code,
-                                          quartic_repeats=number_of_quartic_repeats)
+                state["plan"] = with_mode(_lib.Plan(generators, W, nodes, residual=use_residual,
+                                                    expm=expm_code,
+                                                    quartic_repeats=number_of_quartic_repeats))
             return state["plan"]
         if state["plan"] is None or state["h"] != fine_step:
             gn, dl, sl = rotating_tables(generators, doubles, singles, nodes, fine_step,
@@ -194,6 +222,7 @@ def generate_simulator(
                                                     singles_last=sl,
                                                     vectors_real=vectors_real,
                                                     inv_vectors_real=inv_vectors_real))
+            with_mode(state["plan"])
             state["h"] = fine_step
         return state["plan"]
 
@@ -204,7 +233,10 @@ def generate_simulator(
         time = time_start + time_step*(np.arange(T) + 1)
         if T <= 0:
             return time, np.zeros((0, n, n), dtype=np.complex128)
-        flat0 = flatten_density(rho0, N, vmap)[None]
+        flat0 = flatten_density(rho0, Ns, vmap)[None]
+        if N > PLAIN_MAX_N and (use_kernel or use_unitary):
+            raise NotImplementedError(
+                f"N = {N} > {PLAIN_MAX_N}: kernel and unitary modes run on the dense path only")
         if N > PLAIN_MAX_N:
             # larger than the dense shared-memory propagator path: the same
             # integrator through the batched kernel, full state per sample

@@ -470,8 +470,6 @@ def generate_atoms(description, atom_interactions, block_interactions, use_unita
     the real (N, N) superoperators L0, Gx, Gy, Gz, Gr; ``valid_indices`` is
     the (N, 3) vectorisation map (rows y, x, c).
     """
-    if use_unitary:
-        raise NotImplementedError("the unitary representation is not implemented")
     P = params or default_params
     if not use_hermitian:
         use_incoherent = False
@@ -526,6 +524,15 @@ def generate_atoms(description, atom_interactions, block_interactions, use_unita
     if not use_incoherent:
         allowed[:] = 1
     valid = valid_indices_from_mask(allowed)
+    if use_unitary and not jumps:
+        # closed system: operator generators and the basis change matrices
+        # (generate_generators.py:120-139); no superoperators
+        unitary = {k: complex_to_real(coherent.get(k, np.zeros((n, n), complex)))
+                   for k in ("H0", "Gx", "Gy", "Gz", "Z")}
+        unitary["Gr"] = np.zeros((2*n, 2*n))
+        elim, dup = elimination_matrices(n, valid, use_hermitian)
+        return {"unitary": unitary, "elimination": {"elimination": elim, "duplication": dup},
+                "coherent": coherent, "jump": jumps, "allowed": allowed}, valid
     basis, sel = _basis(n, valid, use_hermitian)
 
     supers = {}
@@ -575,3 +582,104 @@ def _group(supers):
         out[k] = supers.get(k, zero.copy())
     out["Gr"] = totals.get("Gr", zero.copy())
     return out
+
+
+# ---------------------------------------------------------------------------
+# unitary representation
+# ---------------------------------------------------------------------------
+
+def complex_to_real(H):
+    """Real 2n x 2n form of i*H acting on interleaved (re, im) vectors: entry
+    (i, j) of the complex matrix iH sits at [2i][2j] (real part) and
+    [2i+1][2j] (imaginary part), with [2i][2j+1] = -imag and [2i+1][2j+1] =
+    real.  This is the reference's operator generator
+    (generate_generators.py:2725-2746), the real form of +iH."""
+    Z = 1j*np.asarray(H, dtype=complex)
+    n = Z.shape[0]
+    out = np.empty((2*n, 2*n))
+    out[::2, ::2] = Z.real
+    out[1::2, ::2] = Z.imag
+    out[::2, 1::2] = -Z.imag
+    out[1::2, 1::2] = Z.real
+    return out
+
+
+def elimination_matrices(n, valid_indices, use_hermitian):
+    """Elimination (N_h x 2n^2) and duplication (2n^2 x N_h) matrices between
+    the Hermitian basis of the vectorisation map and the full basis of all
+    (y, x, re/im) entries listed column-major, each entry the overlap of two
+    basis matrices over the squared norm of the first
+    (generate_generators.py:2797-2840)."""
+    full = np.zeros((2*n*n, n, n, 2))
+    k = 0
+    for x in range(n):
+        for y in range(n):
+            for c in range(2):
+                full[k, y, x, c] = 1.0
+                k += 1
+    if use_hermitian:
+        herm = np.zeros((len(valid_indices), n, n, 2))
+        for i, (y, x, c) in enumerate(valid_indices):
+            herm[i, y, x, c] = 1.0
+            if y != x:
+                herm[i, x, y, c] = -1.0 if c else 1.0
+    else:
+        herm = full.copy()
+    fh = herm.reshape(len(herm), -1)
+    ff = full.reshape(len(full), -1)
+    elim = (fh @ ff.T)/np.sum(fh**2, axis=1)[:, None]
+    dup = (ff @ fh.T)/np.sum(ff**2, axis=1)[:, None]
+    return elim, dup
+
+
+# ---------------------------------------------------------------------------
+# equivalence classes (common kernel of the generators)
+# ---------------------------------------------------------------------------
+
+def _gram_schmidt(vectors, avoid=(), tolerance=1e-14):
+    out = []
+    for v in vectors:
+        v = np.array(v, dtype=np.float64)
+        for d in avoid:
+            v -= np.dot(d, v)*d
+        for d in out:
+            v -= np.dot(d, v)*d
+        nrm = np.linalg.norm(v)
+        if nrm < tolerance:
+            continue
+        out.append(v/nrm)
+    return out
+
+
+def find_kernel(generators, rtol=1e-9):
+    """(full basis, image basis, generators on the image) for the common
+    kernel of the generators (reference generate_generators.py:2691-2719).
+
+    The reference takes each generator's kernel from eigenvectors with
+    |lambda| <= max|lambda|/1e9, makes the bases real and intersects them
+    (Zassenhaus).  The common kernel is the null space of the stacked
+    generators, found here by SVD of the generators scaled to unit norm with
+    the same relative threshold.  The image basis is then Gram-Schmidt of the
+    identity's columns against the kernel, as the reference's
+    _find_orthogonal does (:2667-2688), and the generators are restricted to
+    it: image^T G image.  Without a common kernel all three are the
+    identity / the generators themselves."""
+    gens = [np.asarray(g, dtype=np.float64) for g in generators]
+    N = gens[0].shape[0]
+    rows = [g/np.linalg.norm(g, 2) for g in gens if np.any(g != 0)]
+    if not rows:
+        kernel = np.eye(N)
+    else:
+        _, sv, vt = np.linalg.svd(np.vstack(rows))
+        sv = np.concatenate([sv, np.zeros(N - sv.size)])
+        kernel = vt[sv <= rtol*sv.max()]
+    if len(kernel) == 0:
+        return np.eye(N), np.eye(N), gens
+    # orient each kernel vector with a positive leading entry, as the
+    # reference's row-echelon basis comes out
+    kernel = np.array([k if k[np.argmax(np.abs(k) > 1e-12)] > 0 else -k for k in kernel])
+    korth = _gram_schmidt(kernel)
+    image = _gram_schmidt(np.eye(N), korth)
+    image_a = np.array(image).T
+    full = np.array(image + korth).T
+    return full, image_a, [image_a.T @ g @ image_a for g in gens]

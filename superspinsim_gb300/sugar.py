@@ -9,7 +9,7 @@ sampled on the host -- or a ``Program`` evaluated on the GPU.
 import numpy as np
 
 from superspinsim_gb300.generate_simulator import generate_simulator
-from superspinsim_gb300.generators import generate_atoms
+from superspinsim_gb300.generators import find_kernel, generate_atoms
 from superspinsim_gb300.program import Program
 from superspinsim_gb300.rotating import RotatingFrameError, make_rotating
 
@@ -45,14 +45,33 @@ def simspins(coefficients, time_start, time_end, time_step, spins, spin_interact
              use_residual=True, use_kernel=False, use_unitary=False, use_cuda=True,
              use_hermitian=True, use_incoherent=True, datatype=np.float64, verbose=False,
              expm="taylor"):
-    """Simulate a spin description; returns (time (T,), density (T, n, n))."""
-    if use_kernel:
-        raise NotImplementedError("equivalence-class (use_kernel) mode is not implemented")
-    if use_unitary:
-        raise NotImplementedError("unitary (use_unitary) mode is not implemented")
+    """Simulate a spin description; returns (time (T,), density (T, n, n)).
+
+    As the reference (sugar.py:472-534): ``use_unitary`` takes the operator
+    generators when the system has no jump operators (else the Liouvillian
+    ones), ``use_kernel`` restricts the generators to the complement of
+    their common kernel, and the rotating frame is built on what results."""
     ops, vmap = generate_atoms(spins, spin_interactions, group_interactions,
-                               use_hermitian=use_hermitian, use_incoherent=use_incoherent)
-    gens = [ops["generators"][k] for k in LABELS]
+                               use_unitary=use_unitary, use_hermitian=use_hermitian,
+                               use_incoherent=use_incoherent)
+    if use_unitary and "unitary" not in ops:
+        use_unitary = False
+    unitary = {}
+    if use_unitary:
+        gens = [ops["unitary"][k] for k in ("H0", "Gx", "Gy", "Gz", "Gr")]
+        unitary = dict(ops["elimination"])
+    else:
+        gens = [ops["generators"][k] for k in LABELS]
+    kernel = {}
+    if use_kernel:
+        full, image, gens_image = find_kernel(gens)
+        if image.shape[1] == image.shape[0]:
+            use_kernel = False      # no common kernel: nothing to remove
+        elif use_unitary:
+            raise NotImplementedError("kernel and unitary modes together are not supported")
+        else:
+            gens = gens_image
+            kernel = dict(full_projection=full, image_projection=image)
     rotating = {}
     if use_rotating:
         if np.sum(np.abs(gens[0])) == 0:
@@ -71,7 +90,8 @@ def simspins(coefficients, time_start, time_end, time_step, spins, spin_interact
         use_residual=use_residual, number_of_quartic_repeats=number_of_quadratic_repeats,
         number_of_exponentials=number_of_exponentials,
         number_of_fine_divisions=number_of_fine_divisions, use_rotating=use_rotating,
-        use_hermitian=use_hermitian, verbose=verbose, expm=expm, **rotating)
+        use_hermitian=use_hermitian, verbose=verbose, expm=expm, use_kernel=use_kernel,
+        use_unitary=use_unitary, **rotating, **kernel, **unitary)
     return sim(density_initial, time_start, time_end, time_step)
 
 

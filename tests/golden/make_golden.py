@@ -443,6 +443,31 @@ def save_case(c, extra_runs=()):
           f"{_time.time() - t_start:.1f} s", flush=True)
 
 
+def save_modes():
+    """Operator (unitary) generators, elimination/duplication matrices and
+    the equivalence-class projection of the reference for the qubit, qutrit
+    and hyperfine systems (``generate_generators.py:120-139``, ``find_kernel``
+    :2691-2719), as ``modes_<system>.npz``."""
+    from superspinsim.generate_generators import generate_atoms, find_kernel
+    for name, spins in (("qubit", QUBIT), ("qutrit", QUTRIT), ("qubit_hf", QUBIT_HF)):
+        arrays = {}
+        g, vmap = generate_atoms(spins, [{}], {}, True, True, True)
+        for k in ("H0", "Gx", "Gy", "Gz", "Gr"):
+            arrays["unitary_" + k] = g["unitary"][k]
+        arrays["elimination"] = g["elimination"]["elimination"]
+        arrays["duplication"] = g["elimination"]["duplication"]
+        arrays["vectorisation_map"] = vmap
+        g, vmap = generate_atoms(spins, [{}], {}, False, True, True)
+        gens = [g["generators"][k] for k in ["L0", "Gx", "Gy", "Gz", "Gr"]]
+        full, image, gens_image = find_kernel(gens)
+        arrays["generators"] = np.array(gens)
+        arrays["full_projection"] = full
+        arrays["image_projection"] = image
+        arrays["generators_image"] = np.array(gens_image)
+        np.savez_compressed(os.path.join(HERE, f"modes_{name}.npz"), **arrays)
+        print(f"modes_{name}: N={gens[0].shape[0]} r={image.shape[1]}", flush=True)
+
+
 def save_quadratures():
     """The reference's Gauss-Legendre nodes and commutator-free weights
     (``superspinsim/quadratures.py:10-50``)."""
@@ -458,6 +483,9 @@ def save_quadratures():
 def main():
     install_shim()
     only = set(sys.argv[1:])
+    if "modes" in only:
+        save_modes()
+        return
     save_quadratures()
     for c in cases():
         if only and c["name"] not in only:

@@ -52,9 +52,48 @@ def test_lindbladian_properties():
         assert np.abs(diag @ g["generators"][k]).max() <= 1e-6*max(1, np.abs(g["generators"][k]).max())*1e-6
 
 
-def test_unsupported_raise():
-    with pytest.raises(NotImplementedError):
-        generate_atoms([[{"S": 1}]], [{}], {}, use_unitary=True)
+@pytest.mark.parametrize("name", ["qubit", "qutrit", "qubit_hf"])
+def test_unitary_generators_and_elimination_match_reference(name):
+    """Operator generators (real form of +iH), elimination/duplication
+    matrices and the map, against the reference's own output."""
+    import make_golden as mg
+    spins = {"qubit": mg.QUBIT, "qutrit": mg.QUTRIT, "qubit_hf": mg.QUBIT_HF}[name]
+    z = np.load(os.path.join(GOLDEN, f"modes_{name}.npz"))
+    ops, vm = generate_atoms(spins, [{}], {}, use_unitary=True)
+    for k in ("H0", "Gx", "Gy", "Gz", "Gr"):
+        assert np.array_equal(ops["unitary"][k], z["unitary_" + k]), k
+    assert np.array_equal(ops["elimination"]["elimination"], z["elimination"])
+    assert np.array_equal(ops["elimination"]["duplication"], z["duplication"])
+    assert np.array_equal(vm, z["vectorisation_map"])
+
+
+def test_unitary_falls_back_with_jump_operators():
+    ops, _ = generate_atoms([[{"S": 1/2, "g": 2.0, "B0": np.array([0, 0, 1e-3]),
+                               "TS2": 1e-6}]], [{}], {}, use_unitary=True)
+    assert "unitary" not in ops and "generators" in ops
+
+
+@pytest.mark.parametrize("name", ["qubit", "qutrit", "qubit_hf"])
+def test_find_kernel_matches_reference(name):
+    """Image basis and projected generators against the reference's
+    find_kernel.  On the hyperfine qubit the reference finds no common
+    kernel although the identity direction is annihilated by every
+    generator; there the restatement removes it (r = 15), and the
+    projection is exact, so both give the same dynamics."""
+    from superspinsim_gb300.generators import find_kernel
+    z = np.load(os.path.join(GOLDEN, f"modes_{name}.npz"))
+    gens = z["generators"]
+    full, image, gi = find_kernel(list(gens))
+    if name == "qubit_hf":
+        assert z["image_projection"].shape[1] == 16 and image.shape[1] == 15
+        k = full[:, 15]
+        for g in gens:
+            assert np.abs(g @ k).max() <= 1e-9*np.abs(g).max()
+        return
+    assert np.abs(image - z["image_projection"]).max() <= 1e-14
+    assert np.abs(full - z["full_projection"]).max() <= 1e-14
+    scale = np.abs(gens).max()
+    assert np.abs(np.array(gi) - z["generators_image"]).max() <= 1e-14*scale
 
 
 @pytest.mark.parametrize("name", ["qubit_hyperfine", "qubit_couple_rot_e5", "qutrit_hyperfine"])
