@@ -135,7 +135,11 @@ int sss_simulate_device(sss_plan* plan, int ntraj, const double* rho0, int nch,
  *   samples: ntraj output-sample counts (NULL: all T_max)
  *   host != 0: all pointers are host pointers (copied in and out within the
  *   call); host == 0: device pointers.
- * Uses SSS_EXPM_TAYLOR arithmetic; lab frame only. */
+ * Uses SSS_EXPM_TAYLOR arithmetic.  A rotating plan (SSS_ROTATING, tables
+ * set) runs in the generalised rotating frame on the row-part kernel
+ * (variant 0 or 4): states, weights and outputs stay in the lab basis, the
+ * kernel converting with V and V^-1 (generate_simulator.py:450-532 Omega,
+ * :901-1021 e^{L0 h} blocks, :2030-2038 sandwich). */
 int sss_batch_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                   int nseg, const double* programs, const int* samples,
                   double t0, double dt, int T_max, int F,

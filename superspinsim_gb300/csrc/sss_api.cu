@@ -148,7 +148,7 @@ int sss_plan_set_rotating(sss_plan* p, const double* gn, const double* dlast, in
     if (int rc = upload(p->d_slast, p->slast.data(), p->slast.size())) return rc;
     if (int rc = upload(p->d_V, V, NN)) return rc;
     if (int rc = upload(p->d_Vinv, Vinv, NN)) return rc;
-    return SSS_OK;
+    return build_sparse(p);  // (node, generator) slots for batched runs
 }
 
 int sss_plan_set_projection(sss_plan* p, int n_full, const double* P) {
@@ -275,7 +275,7 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
                                    : (final_state ? (const void*)final_state : (const void*)trace)))
         return rc;
     if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
-    if (p->rotating) return fail(SSS_EINVAL, "batched runs support the lab frame only");
+    if (p->rotating && p->D + p->S == 0) return fail(SSS_EINVAL, "rotating tables not set");
     if (p->n_full || p->u_n)
         return fail(SSS_EINVAL, "batched runs support neither projected nor unitary plans");
     if (readout && !readout_weights) return fail(SSS_EINVAL, "readout needs readout_weights");
@@ -408,7 +408,7 @@ int sss_batch_prepare(sss_plan* p, int ntraj, const double* rho0, int nch, int n
                       void* stream) {
     if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, 1, F, rho0)) return rc;
     if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
-    if (p->rotating) return fail(SSS_EINVAL, "batched runs support the lab frame only");
+    if (p->rotating && p->D + p->S == 0) return fail(SSS_EINVAL, "rotating tables not set");
     if (p->n_full || p->u_n)
         return fail(SSS_EINVAL, "batched runs support neither projected nor unitary plans");
     if (ntraj == 0) return fail(SSS_EINVAL, "empty batch");

@@ -55,8 +55,19 @@ namespace sss {
 // ---------------------------------------------------------------------------
 
 int build_sparse(sss_plan* p) {
-    const int N = p->d.N, G = p->d.G;
+    // lab plans: G generators; rotating plans: Q*G (node, generator) slots,
+    // whose entries below 1e-16 of the slot's largest (the rounding left by
+    // the basis change) are dropped
+    const int N = p->d.N, G = p->rotating ? p->d.Q * p->d.G : p->d.G;
     SparseGenerators& s = p->sparse;
+    std::vector<double> drop(G, 0.0);
+    if (p->rotating)
+        for (int g = 0; g < G; g++) {
+            double mx = 0.0;
+            for (size_t i = 0; i < (size_t)N * N; i++)
+                mx = std::max(mx, std::fabs(p->gens[(size_t)g * N * N + i]));
+            drop[g] = 1e-16 * mx;
+        }
     s.N = N;
     s.G = G;
     s.row_ptr.assign(N + 1, 0);
@@ -66,10 +77,13 @@ int build_sparse(sss_plan* p) {
         for (int c = 0; c < N; c++) {
             bool nz = false;
             for (int g = 0; g < G; g++)
-                if (p->gens[((size_t)g * N + r) * N + c] != 0.0) nz = true;
+                if (std::fabs(p->gens[((size_t)g * N + r) * N + c]) > drop[g]) nz = true;
             if (!nz) continue;
             s.col.push_back(c);
-            for (int g = 0; g < G; g++) vals[g].push_back(p->gens[((size_t)g * N + r) * N + c]);
+            for (int g = 0; g < G; g++) {
+                const double v = p->gens[((size_t)g * N + r) * N + c];
+                vals[g].push_back(std::fabs(v) > drop[g] ? v : 0.0);
+            }
         }
         s.row_ptr[r + 1] = (int)s.col.size();
     }
@@ -90,7 +104,7 @@ struct BatchArgs {
     int E;        // entries per lane (max over lanes)
     int t_begin, t_end;        // output samples of this launch
     double h_sub, t0, dt;
-    int gen_index[kMaxG];      // active generator -> coefficient slot
+    int gen_index[kMaxSlots];  // active generator -> coefficient slot
     const double* toff;        // F: (r*dt)/F
     const double* noff;        // Q: (dt*node_k)/F
     const double* W;           // K*Q
@@ -113,7 +127,18 @@ struct BatchArgs {
     const double* om0;         // K*C*P*L  constant part of Omega per exponential
     int kc;                    // close slots per lane (max over lanes)
     int n_live;                // generators assembled per step (the others are in om0)
-    int live[kMaxG];           // their active-generator slots
+    int live[kMaxSlots];       // their active-generator slots
+    int live_k[kMaxSlots];     // node of a rotating slot (weight W[e,k] c_k), -1: sum over nodes
+    int live_ch[kMaxSlots];    // index of its channel among the live channels
+    int n_lch;                 // live channels (sampled into the ring)
+    int lch_chan[kMaxSlots];   // their program channel (>= nch: zero)
+    // generalised rotating frame (state in the eigenbasis of L0)
+    int rot, resid;
+    const double* Vm;          // N*N eigenvectors (lab = V x)
+    const double* Vinvm;       // N*N inverse (x = V^-1 rho)
+    const double* blk_self;    // M: e^{L0 h} diagonal coefficient of each row (minus 1 when residual)
+    const double* blk_part;    // M: coefficient of its partner row
+    const int* blk_pos;        // M: the partner's row (M: none, the zero row)
     double* states;            // state before every exponential, or null:
     long st_steps;             //   [((b*st_steps + n)*K + e)*M + row], n = step since t_begin
     double inv_j[kMaxTaylor + 1];
@@ -549,14 +574,14 @@ template <int L, int C, int P>
 __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
     extern __shared__ double smem[];
     constexpr int CP = C * P;
-    const int M = a.M, NL = a.n_live, K = a.K, Q = a.Q;
+    const int M = a.M, NL = a.n_live, NC = a.n_lch, K = a.K, Q = a.Q;
     const int Ms = M + 2;  // rows, the zero row M, the sink row M+1
     const int slot = threadIdx.x / L, li = threadIdx.x % L;
-    const size_t per_slot = (3 * (size_t)Ms + L * C + 1 + (size_t)kRing * (Q + K) * NL) | 1;
+    const size_t per_slot = (3 * (size_t)Ms + L * C + 1 + (size_t)kRing * (Q * NC + K * NL)) | 1;
     double* sbuf = smem + slot * per_slot;
     double* parts = sbuf + 3 * (size_t)Ms;
-    double* ringc = parts + L * C + 1;           // [s][k][live] node values
-    double* ring_ag = ringc + kRing * Q * NL;    // [s][e][live] CF weights
+    double* ringc = parts + L * C + 1;           // [s][k][live channel] node values
+    double* ring_ag = ringc + kRing * Q * NC;    // [s][e][live] CF weights
     double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
     for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
     for (int i = li; i < 3 * Ms; i += L) sbuf[i] = 0.0;
@@ -580,11 +605,24 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
     int b = -1, T_b = 0, t = 0, r = 0, rp = kRing;
     const double* prog = nullptr;
     double om[CP];
+    // rotating frame: the lab-basis state V x, all N entries spread over the lanes
+    auto store_lab = [&](double* dst) {
+        for (int i = li; i < a.N; i += L) {
+            double o = 0.0;
+            for (int row = 0; row < M; row++)
+                o = fma(__ldg(a.Vm + (size_t)i * a.N + __ldg(a.row_orig + row)), v[row], o);
+            dst[i] = o;
+        }
+    };
 
     while (true) {
         if (r == 0 && t >= T_b) {
-            if (b >= 0 && a.fin)
-                for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+            if (b >= 0 && a.fin) {
+                if (a.rot)
+                    store_lab(a.fin + (size_t)b * a.N);
+                else
+                    for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+            }
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
                     a.readout[(size_t)b * a.T_max + tt] = 0.0;
@@ -597,28 +635,46 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             t = a.t_begin;
             rp = kRing;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
-            for (int row = r0; row < r1; row++) v[row] = a.rho0[(size_t)b * a.N + a.row_orig[row]];
+            const double* r0b = a.rho0 + (size_t)b * a.N;
+            if (a.rot) {
+                // eigenbasis coordinates x = V^-1 rho0 on the kept rows
+                for (int row = r0; row < r1; row++) {
+                    const double* vi = a.Vinvm + (size_t)__ldg(a.row_orig + row) * a.N;
+                    double o = 0.0;
+                    for (int j = 0; j < a.N; j++) o = fma(__ldg(vi + j), r0b[j], o);
+                    v[row] = o;
+                }
+            } else {
+                for (int row = r0; row < r1; row++) v[row] = r0b[a.row_orig[row]];
+            }
             __syncwarp(gmask);
             if (t >= T_b) continue;
         }
         if (rp == kRing) {
             // node values of the live channels for fine steps (t, r) .. +kRing-1,
             // node time ((t0 + (r*dt)/F) + dt*t) + (dt*node)/F, each op rounded
-            for (int i = li; i < kRing * Q * NL; i += L) {
-                const int s = i / (Q * NL), rem = i - s * Q * NL, k = rem / NL, gi = rem - k * NL;
+            for (int i = li; i < kRing * Q * NC; i += L) {
+                const int s = i / (Q * NC), rem = i - s * Q * NC, k = rem / NC, ci = rem - k * NC;
                 const int rr = r + s, ts = t + rr / a.F, rs = rr % a.F;
                 const double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + rs)),
                                                       __dmul_rn(a.dt, (double)ts)),
                                             __ldg(a.noff + k));
-                const int g = a.gen_index[a.live[gi]];
-                ringc[i] = (g - 1 < a.nch) ? channel_value(prog, a.nseg, g - 1, tn) : 0.0;
+                const int ch = a.lch_chan[ci];
+                ringc[i] = ch < a.nch ? channel_value(prog, a.nseg, ch, tn) : 0.0;
             }
             __syncwarp(gmask);
+            // CF weights: lab generators sum their channel over the nodes; a
+            // rotating slot belongs to one node k and takes W[e,k] c_k
             for (int i = li; i < kRing * K * NL; i += L) {
                 const int s = i / (K * NL), rem = i - s * K * NL, e = rem / NL, gi = rem - e * NL;
+                const int kk = a.live_k[gi], ci = a.live_ch[gi];
                 double w = 0.0;
-                for (int k = 0; k < Q; k++)
-                    w = fma(__ldg(a.W + e * Q + k), ringc[(s * Q + k) * NL + gi], w);
+                if (kk < 0) {
+                    for (int k = 0; k < Q; k++)
+                        w = fma(__ldg(a.W + e * Q + k), ringc[(s * Q + k) * NC + ci], w);
+                } else {
+                    w = __ldg(a.W + e * Q + kk) * ringc[(s * Q + kk) * NC + ci];
+                }
                 ring_ag[i] = w * a.h_sub;
             }
             __syncwarp(gmask);
@@ -674,12 +730,30 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                 v = cur;
             }
         }
+        if (a.rot) {
+            // e^{L0 h} in the eigenbasis (generate_simulator.py:901-964): 2 x 2
+            // blocks of the complex pairs and the real singles, each row from
+            // itself and its partner; residual form x + (c_s x + c_p x_p)
+            for (int row = r0; row < r1; row++) {
+                const double xs = v[row], xp = v[__ldg(a.blk_pos + row)];
+                const double cs = __ldg(a.blk_self + row), cp = __ldg(a.blk_part + row);
+                x[row] = a.resid ? fma(cp, xp, fma(cs, xs, xs)) : fma(cp, xp, cs * xs);
+            }
+            __syncwarp(gmask);
+            double* tmp = v;
+            v = x;
+            x = tmp;
+        }
         rp++;
         if (++r == a.F) {
             r = 0;
-            if (a.trace)
-                for (int row = r0; row < r1; row++)
-                    a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
+            if (a.trace) {
+                if (a.rot)
+                    store_lab(a.trace + ((size_t)b * a.T_max + t) * a.N);
+                else
+                    for (int row = r0; row < r1; row++)
+                        a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[row]] = v[row];
+            }
             if (a.readout) {
                 double s = 0.0;
                 for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
@@ -930,47 +1004,58 @@ int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::En
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
                  bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts) {
-    const int N = p->d.N, G = p->d.G;
+    const int N = p->d.N;
+    const bool rot = p->rotating;
     BatchLayout& Ly = *out;
     const SparseGenerators& sp = p->sparse;
+    const int G = sp.G;  // generator slots: lab generators, or rotating (node, generator)
+    // program channel of a slot: lab slot g is driven by channel g-1 (slot 0,
+    // L0, has coefficient 1); rotating slot k*G0 + g by channel g
+    auto slot_chan = [&](int a) { return rot ? a % p->d.G : a - 1; };
     std::vector<double> h_rho0((size_t)ntraj * N), h_prog((size_t)ntraj * nch * nseg * 5);
     SSS_CUDA(cudaMemcpyAsync(h_rho0.data(), d_rho0, sizeof(double) * h_rho0.size(),
                              cudaMemcpyDeviceToHost, st));
     SSS_CUDA(cudaMemcpyAsync(h_prog.data(), d_prog, sizeof(double) * h_prog.size(),
                              cudaMemcpyDeviceToHost, st));
     SSS_CUDA(cudaStreamSynchronize(st));
-    // ---- active generators: L0 always; channel c drives generator c+1 ----
-    std::vector<double> cmax(G, 0.0);
-    cmax[0] = 1.0;
-    for (int b = 0; b < ntraj; b++)
-        for (int c = 0; c < nch && c + 1 < G; c++)
-            for (int s = 0; s < nseg; s++) {
-                const double* q = &h_prog[(((size_t)b * nch + c) * nseg + s) * 5];
-                if (q[0] == -INFINITY) continue;  // never matches
-                cmax[c + 1] = std::max(cmax[c + 1], std::fabs(q[1]) + std::fabs(q[2]));
-            }
-    // channels holding one constant value for every trajectory at all times
-    // (every segment of zero amplitude with the same offset, the last one
-    // never ending): the row-part kernel folds them into the constant part
-    // of Omega
-    Ly.chan_const.assign(G, 0);
-    Ly.chan_value.assign(G, 0.0);
-    for (int c = 0; c < nch && c + 1 < G; c++) {
+    // ---- channels: largest |coefficient|, and whether the channel holds one
+    // constant value for every trajectory at all times (every segment of
+    // zero amplitude with the same offset, the last one never ending): the
+    // row-part kernel folds those into the constant part of Omega ----
+    std::vector<double> chmax(std::max(nch, 1), 0.0), chval(std::max(nch, 1), 0.0);
+    std::vector<char> chconst(std::max(nch, 1), 0);
+    for (int c = 0; c < nch; c++) {
         bool ok = ntraj > 0 && nseg > 0;
         double val = 0.0;
-        for (int b = 0; b < ntraj && ok; b++) {
+        for (int b = 0; b < ntraj; b++) {
             const double* seg = &h_prog[((size_t)b * nch + c) * nseg * 5];
             if (!(seg[(size_t)(nseg - 1) * 5] == INFINITY)) ok = false;
-            for (int q = 0; q < nseg && ok; q++) {
+            for (int q = 0; q < nseg; q++) {
                 const double* sq = seg + (size_t)q * 5;
+                if (sq[0] != -INFINITY)  // a segment that can match
+                    chmax[c] = std::max(chmax[c], std::fabs(sq[1]) + std::fabs(sq[2]));
+                if (!ok) continue;
                 if (sq[2] != 0.0 || !(sq[1] == sq[1])) ok = false;
                 else if (b == 0 && q == 0) val = sq[1];
                 else if (sq[1] != val) ok = false;
             }
         }
-        if (ok) {
-            Ly.chan_const[c + 1] = 1;
-            Ly.chan_value[c + 1] = val;
+        chconst[c] = ok;
+        chval[c] = val;
+    }
+    std::vector<double> cmax(G, 0.0);
+    Ly.chan_const.assign(G, 0);
+    Ly.chan_value.assign(G, 0.0);
+    Ly.slot_chan.assign(G, -1);
+    for (int a = 0; a < G; a++) {
+        const int c = slot_chan(a);
+        Ly.slot_chan[a] = c;
+        if (c < 0) {
+            cmax[a] = 1.0;
+        } else if (c < nch) {
+            cmax[a] = chmax[c];
+            Ly.chan_const[a] = chconst[c];
+            Ly.chan_value[a] = chval[c];
         }
     }
     std::vector<int> active;
@@ -981,13 +1066,32 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
         if ((cmax[g] > 0.0 || forced) && nonzero_gen) active.push_back(g);
     }
     const int Ga = (int)active.size();
-    // ---- reachable rows from the initial states' support ----
+    // ---- reachable rows from the initial states' support (in the eigenbasis
+    // for a rotating plan: the entries of V^-1 rho0 above 1e-15 of its
+    // largest), closed under the pattern and, rotating, the e^{L0 h} pairs ----
     std::vector<char> reach(N, 0);
     std::vector<int> stack;
-    for (int b = 0; b < ntraj; b++)
-        for (int i = 0; i < N; i++)
-            if (h_rho0[(size_t)b * N + i] != 0.0 && !reach[i]) { reach[i] = 1; stack.push_back(i); }
+    for (int b = 0; b < ntraj; b++) {
+        const double* r0b = &h_rho0[(size_t)b * N];
+        if (rot) {
+            std::vector<double> xe(N, 0.0);
+            double mx = 0.0;
+            for (int i = 0; i < N; i++) {
+                double o = 0.0;
+                for (int j = 0; j < N; j++) o += p->Vinv[(size_t)i * N + j] * r0b[j];
+                xe[i] = o;
+                mx = std::max(mx, std::fabs(o));
+            }
+            for (int i = 0; i < N; i++)
+                if (std::fabs(xe[i]) > 1e-15 * mx && !reach[i]) { reach[i] = 1; stack.push_back(i); }
+        } else {
+            for (int i = 0; i < N; i++)
+                if (r0b[i] != 0.0 && !reach[i]) { reach[i] = 1; stack.push_back(i); }
+        }
+    }
     std::vector<std::vector<int>> influences(N);
+    if (rot)
+        for (int i = 0; i < 2 * p->D; i++) influences[i].push_back(i ^ 1);
     for (int r = 0; r < N; r++)
         for (int q = sp.row_ptr[r]; q < sp.row_ptr[r + 1]; q++) {
             bool nz = false;
@@ -1035,6 +1139,10 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
         for (int k = 0; k < p->d.Q; k++) s += std::fabs(p->W[e * p->d.Q + k]);
         wsum = std::max(wsum, s);
     }
+    if (rot) {  // a slot's weight is h W[e,k] c: bound sum_k |W[e,k]| by the largest |W|
+        wsum = 0.0;
+        for (int i = 0; i < p->d.K * p->d.Q; i++) wsum = std::max(wsum, std::fabs(p->W[i]));
+    }
     double beta = 0.0;
     for (int g : active) {
         std::vector<double> colsum(M, 0.0);
@@ -1062,7 +1170,9 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
     // Automatic lanes: 32 (one trajectory per warp, the shortest chains)
     // while the batch gives at most two warps per SM sub-partition, else 16
     // (two trajectories per warp, fewer instructions per trajectory)
-    if (force_parts || (allow_register && (p->batch_variant == 4 || p->batch_variant == 0))) {
+    if (rot && !force_parts && allow_register && p->batch_variant != 0 && p->batch_variant != 4)
+        return fail(SSS_EINVAL, "the rotating frame runs on the row-part kernel (variant 0 or 4)");
+    if (force_parts || (allow_register && (rot || p->batch_variant == 4 || p->batch_variant == 0))) {
         const int Lp = p->batch_lanes > 0 && !force_parts
                            ? L
                            : ((long)ntraj <= 8L * p->num_sms ? 32 : 16);
@@ -1074,7 +1184,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
             Ly.degree = degree;
             Ly.substeps = substeps;
         }
-        if (rc == SSS_OK || p->batch_variant == 4 || force_parts) return rc;
+        if (rc == SSS_OK || p->batch_variant == 4 || force_parts || rot) return rc;
     }
     // ---- rows to lanes, balanced by entry count.  The register variant
     // pads each row to an even length (two chains); an empty row carries
@@ -1174,9 +1284,19 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
     const int N = p->d.N;
     const std::vector<int>& active = Ly.active;
     const std::vector<int>& row_orig = Ly.row_orig;
+    const bool rot = p->rotating;
     std::vector<double> rw(M, 0.0);
-    if (h_rw)
-        for (int k = 0; k < M; k++) rw[k] = h_rw[row_orig[k]];
+    if (h_rw) {
+        if (rot) {  // readout of V x: weights V^T w on the kept eigenbasis rows
+            for (int k = 0; k < M; k++) {
+                double o = 0.0;
+                for (int i = 0; i < N; i++) o += h_rw[i] * p->V[(size_t)i * N + row_orig[k]];
+                rw[k] = o;
+            }
+        } else {
+            for (int k = 0; k < M; k++) rw[k] = h_rw[row_orig[k]];
+        }
+    }
     std::vector<double> toff(F), noff(p->d.Q);
     for (int r = 0; r < F; r++) toff[r] = ((double)r * dt) / F;
     for (int k = 0; k < p->d.Q; k++) noff[k] = (dt * p->nodes[k]) / F;
@@ -1188,10 +1308,11 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
     const size_t n_lane_ints = ints.size();
     // row-part variant: the constant part of Omega per exponential -- L0
     // (coefficient 1 in the lab frame) and the channels that are constant
-    // over the batch -- formed as the kernel would (weight sum_k W[e,k]*c,
-    // times h, times the generator, accumulated by FMA in generator order);
-    // the other active generators stay live in the kernel
-    std::vector<int> live;
+    // over the batch -- formed as the kernel would (weight sum_k W[e,k]*c, or
+    // W[e,k]*c for a rotating slot of node k, times h, times the generator,
+    // accumulated by FMA in generator order); the other active generators
+    // stay live in the kernel, their channels sampled into the ring
+    std::vector<int> live, live_k, live_ch, lch;
     const size_t o_om0 = dbl.size();
     if (Ly.parts) {
         const int CP = Ly.C * Ly.P;
@@ -1199,15 +1320,24 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
         std::vector<double> om0((size_t)p->d.K * CP * L, 0.0);
         for (int gi = 0; gi < Ga; gi++) {
             const int g = active[gi];
+            const int ch = Ly.slot_chan[g];
+            const int node = rot ? g / p->d.G : -1;
             const bool keep = std::find(keep_live.begin(), keep_live.end(), g) != keep_live.end();
-            if (g != 0 && (!Ly.chan_const[g] || keep)) {
+            if (ch >= 0 && (!Ly.chan_const[g] || keep)) {
                 live.push_back(gi);
+                live_k.push_back(node);
+                int ci = (int)(std::find(lch.begin(), lch.end(), ch) - lch.begin());
+                if (ci == (int)lch.size()) lch.push_back(ch);
+                live_ch.push_back(ci);
                 continue;
             }
-            const double X = g == 0 ? 1.0 : Ly.chan_value[g];
+            const double X = ch < 0 ? 1.0 : Ly.chan_value[g];
             for (int e = 0; e < p->d.K; e++) {
                 double s = 0.0;
-                for (int k = 0; k < p->d.Q; k++) s = std::fma(p->W[e * p->d.Q + k], X, s);
+                if (node < 0)
+                    for (int k = 0; k < p->d.Q; k++) s = std::fma(p->W[e * p->d.Q + k], X, s);
+                else
+                    s = p->W[e * p->d.Q + node] * X;
                 const double ag = s * h_sub;
                 for (int i = 0; i < CP * L; i++) {
                     double& o = om0[(size_t)e * CP * L + i];
@@ -1221,7 +1351,33 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
     dbl.insert(dbl.end(), rw.begin(), rw.end());
     dbl.insert(dbl.end(), toff.begin(), toff.end());
     dbl.insert(dbl.end(), noff.begin(), noff.end());
+    // rotating frame: e^{L0 h} per kept row -- its own coefficient (minus 1
+    // in residual form, as the plan's tables hold it) and its partner's
+    const size_t o_blk = dbl.size();
+    std::vector<int> blk_pos;
+    if (rot) {
+        std::vector<int> pos_of(N, M);
+        for (int k = 0; k < M; k++) pos_of[row_orig[k]] = k;
+        std::vector<double> bs(M), bp(M, 0.0);
+        blk_pos.assign(M, M);
+        for (int k = 0; k < M; k++) {
+            const int i = row_orig[k];
+            if (i < 2 * p->D) {
+                const double pp = p->dlast[2 * (i / 2)], qq = p->dlast[2 * (i / 2) + 1];
+                bs[k] = pp;
+                bp[k] = (i & 1) ? qq : -qq;
+                blk_pos[k] = pos_of[i ^ 1];
+                if (blk_pos[k] == M) return fail(SSS_EINVAL, "rotating pair split by the pruning");
+            } else {
+                bs[k] = p->slast[i - 2 * p->D];
+            }
+        }
+        dbl.insert(dbl.end(), bs.begin(), bs.end());
+        dbl.insert(dbl.end(), bp.begin(), bp.end());
+    }
     ints.insert(ints.end(), row_orig.begin(), row_orig.end());
+    const size_t o_bpos = ints.size();
+    ints.insert(ints.end(), blk_pos.begin(), blk_pos.end());
     const size_t o_rbeg = ints.size();
     {
         int k = 0;
@@ -1266,7 +1422,22 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
         a.om0 = dv + o_om0;
         a.kc = Ly.kc;
         a.n_live = (int)live.size();
-        for (size_t i = 0; i < live.size(); i++) a.live[i] = live[i];
+        for (size_t i = 0; i < live.size(); i++) {
+            a.live[i] = live[i];
+            a.live_k[i] = live_k[i];
+            a.live_ch[i] = live_ch[i];
+        }
+        a.n_lch = (int)lch.size();
+        for (size_t i = 0; i < lch.size(); i++) a.lch_chan[i] = lch[i];
+    }
+    a.rot = rot ? 1 : 0;
+    a.resid = (p->d.flags & SSS_RESIDUAL) ? 1 : 0;
+    if (rot) {
+        a.Vm = p->d_V.as<double>();
+        a.Vinvm = p->d_Vinv.as<double>();
+        a.blk_self = dv + o_blk;
+        a.blk_part = dv + o_blk + M;
+        a.blk_pos = di + o_bpos;
     }
     a.rho0 = nullptr; a.prog = nullptr; a.samples = nullptr;
     a.readout = nullptr; a.fin = nullptr;
@@ -1276,7 +1447,7 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
     *out = a;
     if (Ly.parts) {
         const size_t per_slot = (3 * (size_t)(M + 2) + L * Ly.C + 1 +
-                                 (size_t)kRing * (p->d.Q + p->d.K) * live.size()) | 1;
+                                 (size_t)kRing * (p->d.Q * lch.size() + p->d.K * live.size())) | 1;
         *smem = sizeof(double) * ((threads / L) * per_slot + M);
     } else if (use_reg) {
         const size_t per_slot = ((one_chain ? 4 : 5) * (size_t)M + kMaxQ * kMaxG) | 1;

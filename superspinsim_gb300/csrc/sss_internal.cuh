@@ -14,6 +14,7 @@ constexpr int kMaxG = 8;      // generators per frame
 constexpr int kMaxQ = 3;      // Gauss-Legendre nodes
 constexpr int kMaxK = 6;      // exponentials per step
 constexpr int kMaxCh = 4;     // coefficient channels
+constexpr int kMaxSlots = kMaxQ * kMaxG;  // generator slots of a rotating plan (node, generator)
 constexpr int kPlainMaxN = 52;  // dense shared-memory propagator path
 // row-part kernels (forward and adjoint)
 constexpr int kCloseMax = 8;    // close slots per lane
@@ -70,8 +71,9 @@ struct BatchLayout {
     int C = 0, P = 0, kc = 0;
     std::vector<int> pcol;                   // C*P*L part entry columns [e][l]
     std::vector<unsigned> cw;                // kCloseMax*L close words [k][l]
-    std::vector<char> chan_const;            // per generator: its channel is batch-constant
+    std::vector<char> chan_const;            // per generator slot: its channel is batch-constant
     std::vector<double> chan_value;          // that constant
+    std::vector<int> slot_chan;              // per generator slot: its program channel (-1: L0)
 };
 
 }  // namespace sss

@@ -240,10 +240,9 @@ def generate_simulator(
         if N > PLAIN_MAX_N:
             # larger than the dense shared-memory propagator path: the same
             # integrator through the batched kernel, full state per sample
-            if use_rotating or expm != "taylor":
+            if expm != "taylor":
                 raise NotImplementedError(
-                    f"N = {N} > {PLAIN_MAX_N}: only the lab frame with expm='taylor' is "
-                    "supported at this size")
+                    f"N = {N} > {PLAIN_MAX_N}: only expm='taylor' is supported at this size")
             if not isinstance(sampler, (Program, np.ndarray)):
                 raise NotImplementedError(
                     f"N = {N} > {PLAIN_MAX_N}: pass the coefficients as a Program")

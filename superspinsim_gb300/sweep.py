@@ -36,17 +36,50 @@ def trapezoid(readout, dt, initial=None):
 
 
 class Sweep:
-    """A batched simulator for lab-frame generators (G, N, N)."""
+    """A batched simulator for lab-frame generators (G, N, N).
+
+    With ``use_rotating`` the batch runs in the reference's generalised
+    rotating frame (``make_rotating`` of L0; simspins' default,
+    superspinsim/sugar.py:536-558): the frame's step tables depend on the
+    fine step, so ``time_step`` is needed up front, and ``run`` with another
+    time step rebuilds the plan.  States, readout weights and results stay
+    in the lab basis."""
 
     def __init__(self, generators, vectorisation_map=None, number_of_exponentials=2,
-                 number_of_fine_divisions=1, lanes=0, cta_threads=0, variant=0):
+                 number_of_fine_divisions=1, lanes=0, cta_threads=0, variant=0,
+                 use_rotating=False, time_step=None, use_residual=True):
         self.generators = np.ascontiguousarray(generators, dtype=np.float64)
         self.vectorisation_map = vectorisation_map
         self.N = self.generators.shape[1]
         self.F = int(number_of_fine_divisions)
-        W, nodes = method(number_of_exponentials)
-        self.plan = _lib.Plan(self.generators, W, nodes)
-        self.plan.set_batch_config(lanes, cta_threads, variant)
+        self.W, self.nodes = method(number_of_exponentials)
+        self.residual = use_residual
+        self._config = (lanes, cta_threads, variant)
+        self.rotating = None
+        if use_rotating:
+            if time_step is None:
+                raise ValueError("a rotating-frame sweep needs its time_step")
+            from superspinsim_gb300.rotating import make_rotating
+            new, V, Vi, d, s = make_rotating(self.generators[0], list(self.generators[1:]))
+            self.rotating = dict(generators=np.array(new), vectors_real=V, inv_vectors_real=Vi,
+                                 doubles=d, singles=s)
+        self.time_step = None
+        self._make_plan(time_step)
+
+    def _make_plan(self, time_step):
+        if self.rotating is None:
+            self.plan = _lib.Plan(self.generators, self.W, self.nodes, residual=self.residual)
+        else:
+            from superspinsim_gb300.generate_simulator import rotating_tables
+            r = self.rotating
+            gn, dl, sl = rotating_tables(r["generators"], r["doubles"], r["singles"], self.nodes,
+                                         time_step/self.F, self.residual)
+            self.plan = _lib.Plan(None, self.W, self.nodes, residual=self.residual,
+                                  rotating=dict(generators_nodes=gn, doubles_last=dl,
+                                                singles_last=sl, vectors_real=r["vectors_real"],
+                                                inv_vectors_real=r["inv_vectors_real"]))
+        self.time_step = time_step
+        self.plan.set_batch_config(*self._config)
 
     def flatten(self, rho0):
         rho0 = np.asarray(rho0)
@@ -68,6 +101,8 @@ class Sweep:
         if flat.shape[0] == 1 and progs.shape[0] > 1:
             flat = np.repeat(flat, progs.shape[0], axis=0)
         T = number_of_samples(time_start, time_end, time_step)
+        if self.rotating is not None and time_step != self.time_step:
+            self._make_plan(time_step)
         ro, fin = self.plan.batch(flat, progs, time_start, time_step, T, self.F,
                                   samples=samples, readout_weights=readout_weights,
                                   want_final=final_state)
