@@ -326,6 +326,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="odmr", choices=["odmr", "ramsey", "nv21", "adjoint"])
     ap.add_argument("--n-traj", type=int, default=0)
+    ap.add_argument("--rotating", action="store_true",
+                    help="run the batch in the generalised rotating frame (simspins' default)")
     args = ap.parse_args()
     rank, world = dist_setup()
     if args.impl == "reference":
@@ -348,7 +350,9 @@ def main():
     rho0 = np.repeat(flatten_density(rho, N, vm)[None], B, axis=0)
     w = population_weights(vm, levels)
     sweep = Sweep(gens, vm, number_of_exponentials=K_EXP, number_of_fine_divisions=F,
-                  lanes=args.lanes, cta_threads=args.threads, variant=args.variant)
+                  lanes=args.lanes, cta_threads=args.threads, variant=args.variant,
+                  use_rotating=args.rotating, time_step=DT_OUT)
+    wdesc["frame"] = "rotating" if args.rotating else "lab"
     plan = sweep.plan
     tuned = None
     if not (args.lanes or args.threads or args.variant):
