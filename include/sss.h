@@ -220,7 +220,8 @@ int sss_plan_set_unitary(sss_plan* plan, int n, int nd, const int* map);
 int sss_plan_last_launches(const sss_plan* plan);
 
 /* Batched-kernel configuration (the autotuner's knobs): lanes per
- * trajectory (1, 2, 4, 8, 16, 32; 0 = automatic), CTA size (a multiple of
+ * trajectory (1, 2, 4, ..., 256; 0 = automatic; above 32 the row-part
+ * variant only, one trajectory per CTA of that many threads), CTA size (a multiple of
  * 32 up to 256; 0 = 32 for the row-part variant, else 64) and variant
  * (0 = automatic: the row-part variant when the pattern fits, else as 1;
  * 1 = register variant when the per-lane share fits, else shared memory;

@@ -472,9 +472,10 @@ int sss_fp64_peak(double* tflops, void* stream) {
 
 int sss_plan_set_batch_config(sss_plan* p, int lanes, int cta_threads, int variant) {
     if (!p) return fail(SSS_EINVAL, "null plan");
-    if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 &&
-        lanes != 32)
-        return fail(SSS_EINVAL, "lanes must be 0 (automatic) or a power of two up to 32");
+    if (lanes < 0 || lanes > 256 || (lanes & (lanes - 1)))
+        return fail(SSS_EINVAL, "lanes must be 0 (automatic) or a power of two up to 256");
+    if (lanes > 32 && variant != 0 && variant != 4)
+        return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part variant");
     if (cta_threads != 0 && (cta_threads < 32 || cta_threads > 256 || cta_threads % 32))
         return fail(SSS_EINVAL, "cta_threads must be 0 or a multiple of 32 in [32, 256]");
     if (variant < 0 || variant > 4) return fail(SSS_EINVAL, "variant must be 0, 1, 2, 3 or 4");

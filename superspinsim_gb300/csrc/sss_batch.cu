@@ -596,9 +596,30 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
     const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
     __syncthreads();
 
+    // a group of L <= 32 lanes lives in one warp (warp barriers and
+    // shuffles); a wider group is the whole CTA (CTA barriers, shared memory)
+    constexpr bool kCta = L > 32;
     const unsigned lane_in_warp = threadIdx.x & 31;
-    const unsigned leader = lane_in_warp / L * L;
-    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    const unsigned leader = kCta ? 0u : lane_in_warp / L * L;
+    const unsigned gmask = (L >= 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    __shared__ int s_bcast;
+    __shared__ double s_red[kCta ? L / 32 : 1];
+    auto gsync = [&]() {
+        if (kCta) __syncthreads(); else __syncwarp(gmask);
+    };
+    // sum over the group, valid in lane 0
+    auto gsum = [&](double v) {
+#pragma unroll
+        for (int o = (L < 32 ? L : 32) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
+        if (kCta) {
+            if (lane_in_warp == 0) s_red[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int w = 1; w < L / 32; w++) v += s_red[w];
+            __syncthreads();
+        }
+        return v;
+    };
     double* v = sbuf;
     double* x = sbuf + Ms;
     double* y = x + Ms;
@@ -628,7 +649,14 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                     a.readout[(size_t)b * a.T_max + tt] = 0.0;
             int nb = 0;
             if (li == 0) nb = atomicAdd(a.queue, 1);
-            nb = __shfl_sync(gmask, nb, leader);
+            if (kCta) {
+                if (li == 0) s_bcast = nb;
+                __syncthreads();
+                nb = s_bcast;
+                __syncthreads();
+            } else {
+                nb = __shfl_sync(gmask, nb, leader);
+            }
             b = nb;
             if (b >= a.ntraj) break;
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
@@ -647,7 +675,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             } else {
                 for (int row = r0; row < r1; row++) v[row] = r0b[a.row_orig[row]];
             }
-            __syncwarp(gmask);
+            gsync();
             if (t >= T_b) continue;
         }
         if (rp == kRing) {
@@ -662,7 +690,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                 const int ch = a.lch_chan[ci];
                 ringc[i] = ch < a.nch ? channel_value(prog, a.nseg, ch, tn) : 0.0;
             }
-            __syncwarp(gmask);
+            gsync();
             // CF weights: lab generators sum their channel over the nodes; a
             // rotating slot belongs to one node k and takes W[e,k] c_k
             for (int i = li; i < kRing * K * NL; i += L) {
@@ -677,7 +705,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                 }
                 ring_ag[i] = w * a.h_sub;
             }
-            __syncwarp(gmask);
+            gsync();
             rp = 0;
         }
         for (int e_exp = K - 1; e_exp >= 0; e_exp--) {
@@ -710,7 +738,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                         for (int c = 0; c < C; c++) s[c] = fma(om[c * P + q], cur[col[c * P + q]], s[c]);
 #pragma unroll
                     for (int c = 0; c < C; c++) parts[li * C + c] = s[c];
-                    __syncwarp(gmask);
+                    gsync();
                     double acc = 0.0;
 #pragma unroll
                     for (int k = 0; k < kCloseMax; k++) {
@@ -721,7 +749,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                         acc = fma(parts[(w >> 16) & 0x7fffu], ij, base);
                         nxt[row] = acc;
                     }
-                    __syncwarp(gmask);
+                    gsync();
                     cur = nxt;
                     nxt = (nxt == x) ? y : x;
                 }
@@ -739,7 +767,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                 const double cs = __ldg(a.blk_self + row), cp = __ldg(a.blk_part + row);
                 x[row] = a.resid ? fma(cp, xp, fma(cs, xs, xs)) : fma(cp, xp, cs * xs);
             }
-            __syncwarp(gmask);
+            gsync();
             double* tmp = v;
             v = x;
             x = tmp;
@@ -757,8 +785,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             if (a.readout) {
                 double s = 0.0;
                 for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
-#pragma unroll
-                for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+                s = gsum(s);
                 if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
             }
             t++;
@@ -877,8 +904,9 @@ int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::En
     BatchLayout& Ly = *out;
     const SparseGenerators& sp = p->sparse;
     const int M = (int)rows.size(), Ga = (int)active.size();
-    if (L != 8 && L != 16 && L != 32)
-        return fail(SSS_EINVAL, "row-part variant needs 8, 16 or 32 lanes per trajectory");
+    if (L != 8 && L != 16 && L != 32 && L != 64 && L != 128 && L != 256)
+        return fail(SSS_EINVAL, "row-part variant needs 8 to 256 lanes per trajectory (a power of two)");
+    if (L > 32) threads = L;  // a group wider than a warp is one CTA
     if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
     auto nparts = [&](int i, int P) { return ((int)rows[i].size() + P - 1) / P; };
     // owners by LPT on close cost; returns kc
@@ -1173,12 +1201,34 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
     if (rot && !force_parts && allow_register && p->batch_variant != 0 && p->batch_variant != 4)
         return fail(SSS_EINVAL, "the rotating frame runs on the row-part kernel (variant 0 or 4)");
     if (force_parts || (allow_register && (rot || p->batch_variant == 4 || p->batch_variant == 0))) {
-        const int Lp = p->batch_lanes > 0 && !force_parts
-                           ? L
-                           : ((long)ntraj <= 8L * p->num_sms ? 32 : 16);
-        const int rc = parts_layout_rows(p, Ly.row_ents, {}, Lp,
-                                         p->batch_threads > 0 ? p->batch_threads : 32, 1, 1, active,
-                                         rows_reached, out, nullptr);
+        // lanes: as configured, or the narrowest group (fewest instructions
+        // per trajectory) that still gives every SM sub-partition a warp and
+        // whose pattern fits; else the widest that fits
+        const int threads_cfg = p->batch_threads > 0 ? p->batch_threads : 32;
+        int rc = SSS_EINVAL;
+        if (p->batch_lanes > 0 && !force_parts) {
+            rc = parts_layout_rows(p, Ly.row_ents, {}, L, threads_cfg, 1, 1, active, rows_reached,
+                                   out, nullptr);
+        } else {
+            int chosen = 0;
+            long parts4 = 0;  // parts of at most 4 entries: lanes beyond twice that stay idle
+            for (const auto& re : Ly.row_ents) parts4 += std::max<long>(1, ((long)re.size() + 3) / 4);
+            for (int Lc : {16, 32, 64, 128, 256}) {
+                if (chosen && Lc > 2 * parts4) break;
+                BatchLayout trial;
+                trial.row_ents = Ly.row_ents;
+                if (parts_layout_rows(p, trial.row_ents, {}, Lc, threads_cfg, 1, 1, active,
+                                      rows_reached, &trial, nullptr) != SSS_OK)
+                    continue;
+                chosen = Lc;
+                if ((long)ntraj * Lc >= 4L * 32 * p->num_sms) break;
+            }
+            if (chosen)
+                rc = parts_layout_rows(p, Ly.row_ents, {}, chosen, threads_cfg, 1, 1, active,
+                                       rows_reached, out, nullptr);
+            else
+                fail(SSS_EINVAL, "row-part variant does not fit this pattern");
+        }
         if (rc == SSS_OK) {
             Ly.nnz = nnz;
             Ly.degree = degree;
@@ -1186,6 +1236,9 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
         }
         if (rc == SSS_OK || p->batch_variant == 4 || force_parts || rot) return rc;
     }
+    if (L > 32)
+        return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part variant, "
+                                "which does not fit this pattern");
     // ---- rows to lanes, balanced by entry count.  The register variant
     // pads each row to an even length (two chains); an empty row carries
     // zero entries so that it still closes ----
@@ -1551,7 +1604,10 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
         switch (L) {
             case 8: rc = launch_parts<8>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
             case 16: rc = launch_parts<16>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
-            default: rc = launch_parts<32>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+            case 32: rc = launch_parts<32>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+            case 64: rc = launch_parts<64>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+            case 128: rc = launch_parts<128>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+            default: rc = launch_parts<256>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
         }
     } else if (use_reg) {
         switch (L) {
@@ -1617,7 +1673,10 @@ int parts_forward_launch(sss_plan* p, const PartsForward& fw, int ntraj, double*
     switch (fw.L) {
         case 8: return launch_parts<8>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
         case 16: return launch_parts<16>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
-        default: return launch_parts<32>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
+        case 32: return launch_parts<32>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
+        case 64: return launch_parts<64>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
+        case 128: return launch_parts<128>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
+        default: return launch_parts<256>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
     }
 }
 

@@ -22,7 +22,7 @@ def _key(sweep, B, progs):
 
 
 def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, repeats=2,
-             lanes=(0, 8, 16, 32), variants=(1, 3, 4), threads=(32, 64, 128), use_cache=True):
+             lanes=(0, 8, 16, 32, 64, 128), variants=(1, 3, 4), threads=(32, 64, 128), use_cache=True):
     """Pick and set the fastest batch configuration for this sweep and batch.
     Returns {"config": (lanes, variant, threads), "ms_per_traj_step": ...,
     "trials": [...]}."""

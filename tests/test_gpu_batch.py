@@ -29,7 +29,7 @@ def _excited_weights(vmap):
 @pytest.mark.parametrize("name", ["nv7_n49", "nv7_n19"])
 @pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 1), (16, 1),
                                            (0, 2), (8, 2), (0, 3), (32, 3), (0, 4), (8, 4),
-                                           (16, 4), (32, 4)])
+                                           (16, 4), (32, 4), (64, 4), (128, 4)])
 def test_batch_odmr_against_oracle(name, lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
@@ -58,8 +58,8 @@ def test_batch_odmr_against_oracle(name, lanes, variant):
     assert np.abs(ro - ref @ w).max() <= 1e-12
 
 
-@pytest.mark.parametrize("variant", [0, 4])
-def test_batch_uneven_lengths_and_plain_agree(variant):
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (0, 4), (64, 4)])
+def test_batch_uneven_lengths_and_plain_agree(lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
     c = load_case("nv7_n49")
@@ -76,7 +76,7 @@ def test_batch_uneven_lengths_and_plain_agree(variant):
     rho0 = np.stack([oracle.flatten(rho, vm, N)]*B)
     W, nodes = method(2)
     plan = _lib.Plan(c["generators"], W, nodes)
-    plan.set_batch_config(variant=variant)
+    plan.set_batch_config(lanes=lanes, variant=variant)
     w = _excited_weights(vm)
     ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, samples=samples, readout_weights=w,
                          want_final=True)
@@ -143,8 +143,11 @@ def test_batch_ramsey_uneven_against_oracle(lanes, variant):
         assert np.abs(fin[b] - ref[-1]).max() <= 1e-12
 
 
-def test_batch_nv21_against_oracle():
-    """21-level NV with 14N (441 x 441), 4 ODMR trajectories."""
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (32, 1), (128, 4), (256, 4)])
+def test_batch_nv21_against_oracle(lanes, variant):
+    """21-level NV with 14N (441 x 441), 4 ODMR trajectories: the register
+    kernel and the row-part kernel with groups of 4 and 8 warps (one
+    trajectory per CTA)."""
     from superspinsim_gb300 import _lib, protocols
     from superspinsim_gb300.quadratures import method
     c = load_case("nv21_n441")
@@ -159,14 +162,17 @@ def test_batch_nv21_against_oracle():
     W, nodes = method(2)
     T, dt, F = 2, 1e-9, 50
     plan = _lib.Plan(gens, W, nodes)
+    plan.set_batch_config(lanes=lanes, variant=variant)
     ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, want_final=True)
     info = plan.batch_info()
     assert info["rows"] < N
-    # the row-part kernel is for small patterns: 1,475 entries do not fit
-    plan.set_batch_config(lanes=32, variant=4)
+    if lanes:
+        assert info["lanes"] == lanes
+    # at 32 lanes the row parts of 1,475 entries do not fit one warp
+    plan2 = _lib.Plan(gens, W, nodes)
+    plan2.set_batch_config(lanes=32, variant=4)
     with pytest.raises(_lib.SSSError, match="row-part"):
-        plan.batch(rho0, progs, 0.0, dt, T, F, want_final=True)
-    plan.set_batch_config()
+        plan2.batch(rho0, progs, 0.0, dt, T, F, want_final=True)
     _, ref = oracle.simulate(gens, np.stack([rho]*4), 0.0, T*dt + 1e-13, dt, progs, K=2, W=W,
                              nodes=nodes, F=F, vectorisation_map=vm, mode="vector", degree=16,
                              flat_out=True)
