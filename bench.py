@@ -271,18 +271,33 @@ def run_adjoint_workload(args, rank, world):
     import torch
     from superspinsim_gb300 import protocols
     from superspinsim_gb300.adjoint import Objective, trapezoid_weights
-    gens, vm = nv7_model()
+    nv21 = args.workload == "adjoint-nv21"
+    if nv21:
+        # NV-21 (14N) at 50 mT: 32 shapes of 64 segments
+        from superspinsim_gb300 import models
+        from superspinsim_gb300.generators import generate_atoms
+        spins, inter, groups = models.nv_21(np.array([0.0, 0.0, 0.05]),
+                                            params=models.nv21_params())
+        g, vm = generate_atoms(spins, inter, groups, use_incoherent=False)
+        gens = np.array([g["generators"][k] for k in ("L0", "Gx", "Gy", "Gz", "Gr")])
+        B, S, f_c = args.n_traj or 32, 64, 2.870e9 + GAMMA*0.05
+        rho = np.zeros((21, 21), complex)
+        for k in range(3, 6):
+            rho[k, k] = 1/3
+        levels = list(range(9, 18))
+    else:
+        gens, vm = nv7_model()
+        B, S, f_c = args.n_traj or 256, 128, F_RES
+        rho = np.zeros((7, 7), complex)
+        rho[1, 1] = 1.0
+        levels = [3, 4, 5]
     rng = np.random.default_rng(20260104)
-    B = args.n_traj or 256
-    S = 128
     rabi = rng.uniform(0, 20e6, (B, S))
     phase = rng.uniform(0, 2*np.pi, (B, S))
-    progs, dur = protocols.pulse_shapes(rabi, phase, 2e-9, F_RES, LASER, 300e-9)
+    progs, dur = protocols.pulse_shapes(rabi, phase, 2e-9, f_c, LASER, 300e-9)
     T = int(round(dur[0]/DT_OUT))
     tw = trapezoid_weights(T, DT_OUT, S*2 - 1, T - 1)
-    rho = np.zeros((7, 7), complex)
-    rho[1, 1] = 1.0
-    obj = Objective(gens, vm, rho, [3, 4, 5], 65.9e6, number_of_exponentials=K_EXP,
+    obj = Objective(gens, vm, rho, levels, 65.9e6, number_of_exponentials=K_EXP,
                     number_of_fine_divisions=F)
     for _ in range(args.warmup):
         obj.run(progs, DT_OUT, T, tw)
@@ -297,12 +312,13 @@ def run_adjoint_workload(args, rank, world):
         adj.append(time.perf_counter() - t)
     fwd_s, adj_s = statistics.median(fwd), statistics.median(adj)
     steps = B*T*F
-    line = {"metric": "NV-7 pulse-shape adjoint gradients/s", "value": B/adj_s,
-            "unit": "gradients/s (256 parameters each)", "n_gpus": world, "steps": args.steps,
+    name = "NV-21" if nv21 else "NV-7"
+    line = {"metric": f"{name} pulse-shape adjoint gradients/s", "value": B/adj_s,
+            "unit": f"gradients/s ({2*S} parameters each)", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3*adj_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{B} pulse shapes x 128 segments of 2 ns + 300 ns readout, "
-                                   "NV-7, dt 5 ps (111,200 steps each)",
+            "config": {"workload": f"{B} pulse shapes x {S} segments of 2 ns + 300 ns readout, "
+                                   f"{name}, dt 5 ps ({T*F:,} steps each)",
                        "parameters_per_shape": 2*S, "traj_steps": steps},
             "adjoint_over_forward": adj_s/fwd_s,
             "forward_traj_steps_per_s": steps/fwd_s,
@@ -324,7 +340,8 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="odmr", choices=["odmr", "ramsey", "nv21", "adjoint"])
+    ap.add_argument("--workload", default="odmr",
+                    choices=["odmr", "ramsey", "nv21", "adjoint", "adjoint-nv21"])
     ap.add_argument("--n-traj", type=int, default=0)
     ap.add_argument("--rotating", action="store_true",
                     help="run the batch in the generalised rotating frame (simspins' default)")
@@ -333,7 +350,7 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
         return
-    if args.workload == "adjoint":
+    if args.workload in ("adjoint", "adjoint-nv21"):
         run_adjoint_workload(args, rank, world)
         return
 

@@ -466,9 +466,29 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
     const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
     __syncthreads();
 
+    // a group of L <= 32 lanes lives in one warp; a wider one is the CTA
+    constexpr bool kCta = L > 32;
     const unsigned lane_in_warp = threadIdx.x & 31;
-    const unsigned leader = lane_in_warp / L * L;
-    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    const unsigned leader = kCta ? 0u : lane_in_warp / L * L;
+    const unsigned gmask = (L >= 32) ? 0xffffffffu : (((1u << L) - 1u) << leader);
+    __shared__ int s_bcast;
+    __shared__ double s_red[kCta ? L / 32 : 1];
+    auto gsync = [&]() {
+        if (kCta) __syncthreads(); else __syncwarp(gmask);
+    };
+    // sum over the group, valid in lane 0
+    auto gsum = [&](double v) {
+#pragma unroll
+        for (int o = (L < 32 ? L : 32) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
+        if (kCta) {
+            if (lane_in_warp == 0) s_red[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int w = 1; w < L / 32; w++) v += s_red[w];
+            __syncthreads();
+        }
+        return v;
+    };
     const double* zb = sb;    // stays zero
     double* mu = sb + Ms;
     double* yA = mu + Ms;
@@ -480,15 +500,22 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
     while (true) {
         int nb = 0;
         if (li == 0) nb = atomicAdd(a.queue, 1);
-        const int b = __shfl_sync(gmask, nb, leader);
+        if (kCta) {
+            if (li == 0) s_bcast = nb;
+            __syncthreads();
+            nb = s_bcast;
+            __syncthreads();
+        } else {
+            nb = __shfl_sync(gmask, nb, leader);
+        }
+        const int b = nb;
         if (b >= a.ntraj) break;
         const double* prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
         // objective from the forward readouts
         {
             double s = 0.0;
             for (int t = li; t < a.T; t += L) s = fma(a.tw[t], a.readout[(size_t)b * a.T + t], s);
-#pragma unroll
-            for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
+            s = gsum(s);
             if (li == 0) a.J[b] = s;
         }
         double* gb = a.grad + (size_t)b * a.nseg * 2;
@@ -502,14 +529,14 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
             acc_p[k] = 0.0;
         }
         for (int row = r0; row < r1; row++) mu[row] = 0.0;
-        __syncwarp(gmask);
+        gsync();
         const double* st_b = a.states + (size_t)b * a.n_steps * K * M;
         int rp = kRing;
         for (long n = a.n_steps - 1; n >= 0; n--) {
             if ((n + 1) % a.F == 0) {
                 const double w = a.tw[(n + 1) / a.F - 1];
                 for (int row = r0; row < r1; row++) mu[row] = fma(w, s_rw[row], mu[row]);
-                __syncwarp(gmask);
+                gsync();
             }
             if (rp == kRing) {
                 // steps n, n-1, ..., n-kRing+1: node values of the live channels;
@@ -547,7 +574,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                         rd[2] = (double)sg;
                     }
                 }
-                __syncwarp(gmask);
+                gsync();
                 for (int i = li; i < kRing * K * NL; i += L) {
                     const int s = i / (K * NL), rem = i - s * K * NL, e = rem / NL, gi = rem - e * NL;
                     double w = 0.0;
@@ -555,7 +582,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                         w = fma(__ldg(a.W + e * Q + k), ringc[(s * Q + k) * NL + gi], w);
                     ring_ag[i] = w * a.h;
                 }
-                __syncwarp(gmask);
+                gsync();
                 rp = 0;
             }
             for (int e_exp = 0; e_exp < K; e_exp++) {
@@ -596,7 +623,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                         parts1[li * C + c] = s1[c];
                         parts2[li * C + c] = s2[c];
                     }
-                    __syncwarp(gmask);
+                    gsync();
                     double a1 = 0.0, a2 = 0.0;
 #pragma unroll
                     for (int k = 0; k < kCloseMax; k++) {
@@ -609,7 +636,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                         pxn[row] = a1;
                         pyn[row] = a2;
                     }
-                    __syncwarp(gmask);
+                    gsync();
                     pxc = pxn;
                     pyc = pyn;
                     pxn = (pxn == xA) ? xB : xA;
@@ -619,8 +646,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                 const double* rb = st_b + ((size_t)n * K + e_exp) * M;
                 double g = 0.0;
                 for (int row = r0; row < r1; row++) g = fma(rb[__ldg(a.fwdpos + row)], pxc[row], g);
-#pragma unroll
-                for (int o = L / 2; o > 0; o >>= 1) g += __shfl_xor_sync(gmask, g, o);
+                g = gsum(g);
                 double* newmu = const_cast<double*>(pyc);
                 if (newmu == yA) yA = mu; else yB = mu;
                 mu = newmu;
@@ -646,7 +672,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                         }
                     }
                 }
-                __syncwarp(gmask);
+                gsync();
             }
             rp++;
         }
@@ -658,7 +684,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                     gb[2 * cur_seg[k] + 1] += acc_p[k];
                 }
         }
-        __syncwarp(gmask);
+        gsync();
     }
 }
 
@@ -724,9 +750,25 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
             prioT[en.col].push_back(sp.val[(size_t)1 * sp.nnz + en.q] != 0.0);
         }
     BatchLayout TL;
-    const int Lb = ntraj <= 8 * p->num_sms ? 32 : 16;
-    const int threads = 32;
-    int ngx = 0;
+    // lanes of the backward groups: the narrowest that fits and gives every
+    // SM sub-partition a warp, else the widest that fits (no wider than twice
+    // the 4-entry parts); one trajectory per CTA above 32 lanes
+    int Lb = 0, ngx = 0;
+    {
+        long parts4 = 0;
+        for (const auto& re : rowsT) parts4 += std::max<long>(1, ((long)re.size() + 3) / 4);
+        for (int Lc : {16, 32, 64, 128, 256}) {
+            if (Lb && Lc > 2 * parts4) break;
+            BatchLayout trial;
+            if (parts_layout_rows(p, rowsT, prioT, Lc, Lc > 32 ? Lc : 32, 3, 2, Ly.active,
+                                  rows_reached, &trial, nullptr) != SSS_OK)
+                continue;
+            Lb = Lc;
+            if ((long)ntraj * Lc >= 4L * 32 * p->num_sms) break;
+        }
+        if (!Lb) return fail(SSS_EINVAL, "the transposed pattern fits no row-part shape");
+    }
+    const int threads = Lb > 32 ? Lb : 32;
     if (int rc = parts_layout_rows(p, rowsT, prioT, Lb, threads, 3, 2, Ly.active, rows_reached, &TL, &ngx))
         return rc;
     const int CP = TL.C * TL.P;
@@ -858,8 +900,14 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
         ab.grad = d_grad + (size_t)b0 * nseg * 2;
         ab.queue = p->w_queue.as<int>();
         SSS_CUDA(cudaMemsetAsync(ab.queue, 0, sizeof(int), st));
-        int rc = Lb == 32 ? launch_adj_parts<32>(p, TL.C, TL.P, ab, threads, smem, st)
-                          : launch_adj_parts<16>(p, TL.C, TL.P, ab, threads, smem, st);
+        int rc;
+        switch (Lb) {
+            case 16: rc = launch_adj_parts<16>(p, TL.C, TL.P, ab, threads, smem, st); break;
+            case 32: rc = launch_adj_parts<32>(p, TL.C, TL.P, ab, threads, smem, st); break;
+            case 64: rc = launch_adj_parts<64>(p, TL.C, TL.P, ab, threads, smem, st); break;
+            case 128: rc = launch_adj_parts<128>(p, TL.C, TL.P, ab, threads, smem, st); break;
+            default: rc = launch_adj_parts<256>(p, TL.C, TL.P, ab, threads, smem, st); break;
+        }
         if (rc) return rc;
         launches += 2;
     }

@@ -148,3 +148,46 @@ def test_adjoint_chunks_and_memory_fallback():
     assert obj.plan.last_launches() == 1
     assert np.abs(J2 - J).max() <= 1e-12*np.abs(J).max()
     assert np.abs(g2 - grad).max() <= 1e-9*np.abs(grad).max()
+
+
+def test_adjoint_nv21_wide_groups_match_fd():
+    """21-level NV with 14N (441 x 441): the row-part adjoint with groups
+    wider than a warp (one trajectory per CTA), J against the forward and
+    the gradient against Richardson-extrapolated central differences."""
+    from superspinsim_gb300 import protocols
+    from superspinsim_gb300.adjoint import Objective, trapezoid_weights
+    c = load_case("nv21_n441")
+    rho = np.zeros((21, 21), complex)
+    for k in range(3, 6):
+        rho[k, k] = 1/3
+    obj = Objective(c["generators"], c["vectorisation_map"], rho, list(range(9, 18)), 65.9e6,
+                    number_of_fine_divisions=50)
+    rng = np.random.default_rng(17)
+    B, S = 2, 2
+    rabi = rng.uniform(5e6, 20e6, (B, S))
+    phase = rng.uniform(0, 2*np.pi, (B, S))
+    f_c = 2.870e9 + 28.025e9*0.05
+    progs, dur = protocols.pulse_shapes(rabi, phase, 1e-9, f_c, 10/65.9, 2e-9)
+    dt = 1e-9
+    T = int(round(dur[0]/dt))
+    tw = trapezoid_weights(T, dt, S - 1, T - 1)
+    J, grad = obj.run(progs, dt, T, tw)
+    assert obj.plan.last_launches() == 2     # row-part forward + backward, no fallback
+    assert obj.plan.batch_info()["lanes"] > 32
+    Jf = obj.forward_only(progs, dt, T, tw)
+    assert np.abs(J - Jf).max() <= 1e-13*np.abs(Jf).max()
+    pert, idx = [], []
+    for b in range(B):
+        for s in range(S):
+            for comp, col, h in ((0, 2, 1e-3*progs[b, 0, s, 2]), (1, 4, 1e-3)):
+                for step in (h, -h, 2*h, -2*h):
+                    p = progs[b].copy()
+                    p[0, s, col] += step
+                    pert.append(p)
+                idx.append((b, s, comp, h))
+    Jp = obj.forward_only(np.stack(pert), dt, T, tw)
+    for k, (b, s, comp, h) in enumerate(idx):
+        d1 = (Jp[4*k] - Jp[4*k + 1])/(2*h)
+        d2 = (Jp[4*k + 2] - Jp[4*k + 3])/(4*h)
+        fd = (4*d1 - d2)/3
+        assert abs(grad[b, s, comp] - fd) <= 1e-7*abs(fd) + 1e-11*abs(J[b])/h, (b, s, comp)
