@@ -208,29 +208,33 @@ def flops_per_traj_step(info, G, K):
     return K*(2*G*nnz + m*d*(2*nnz + 2*rows))
 
 
-def cpu_baseline(steps=None, threads=0):
+CPU_SAMPLES = 16   # output samples of the bounded CPU sample (x F fine steps)
+
+
+def cpu_baseline(steps=None, threads=0, n_freq=N_FREQ):
     """The reference's algorithm (CPU oracle, reference mode) on a bounded
-    sample of the workload: one trajectory, 64 output samples of F = 50
-    fine steps at the workload's 5 ps step (3200 trajectory steps), on all
-    host cores (OpenMP over output samples)."""
+    sample of the workload: its trajectory 0 for 16 output samples of F =
+    200 fine steps at 5 ps (3200 trajectory steps), on all host cores
+    (OpenMP over output samples).  Also returns the flattened states after
+    every sample (key "states"), the reference result of the parity check."""
     from oracle import oracle
     from superspinsim_gb300.quadratures import method
     gens, vm = nv7_model()
-    progs, rho = workload(1)
+    progs, rho = workload(n_freq)
     W, nodes = method(K_EXP)
-    T_s, F_s = 64, 50
-    dt_s = F_s*(DT_OUT/F)
+    T_s = CPU_SAMPLES
     t = time.perf_counter()
-    oracle.simulate(gens, rho, 0.0, T_s*dt_s + dt_s*1e-4, dt_s, progs[0], K=K_EXP, W=W,
-                    nodes=nodes, F=F_s, R=35, residual=True, vectorisation_map=vm,
-                    mode="reference", threads=threads)
+    _, states = oracle.simulate(gens, rho, 0.0, T_s*DT_OUT + DT_OUT*1e-4, DT_OUT, progs[0],
+                                K=K_EXP, W=W, nodes=nodes, F=F, R=35, residual=True,
+                                vectorisation_map=vm, mode="reference", threads=threads,
+                                flat_out=True)
     el = time.perf_counter() - t
-    n = T_s*F_s
+    n = T_s*F
     return {"value": n/el, "unit": "traj-steps/s",
             "cores": threads or oracle.max_threads(), "kind": "port",
-            "sample": f"1 trajectory x {n} CF4:2 steps (64 samples x F=50) of the "
-                      f"workload, reference algorithm (70 squarings per exponential)",
-            "seconds": el}
+            "sample": f"trajectory 0 of the workload, {n} CF4:2 steps ({T_s} samples x F={F}), "
+                      f"reference algorithm (70 squarings per exponential)",
+            "seconds": el, "states": states}
 
 
 def run_reference_arm(args, rank, world):
@@ -247,6 +251,7 @@ def run_reference_arm(args, rank, world):
     cb = dict(samples[0])
     cb["value"] = v
     cb.pop("seconds", None)
+    cb.pop("states", None)
     line = {"metric": METRIC, "value": v, "unit": "traj-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3*total_time/args.steps, "higher_is_better": True,
@@ -490,10 +495,23 @@ def main():
     if args.workload != "odmr":
         line["metric"] = {"ramsey": "NV-7 Ramsey (uneven) traj-steps/s",
                           "nv21": "NV-21 ODMR traj-steps/s"}[args.workload]
-    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "odmr":
-        cb = cpu_baseline()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "odmr" \
+            and not args.rotating:
+        cb = cpu_baseline(n_freq=args.n_freq)
         cb.pop("seconds", None)
+        ref = cb.pop("states")
         line["cpu_baseline"] = cb
+        # parity: the same trajectory and window through the batched path,
+        # against the reference algorithm's states
+        ro_p, _, tr_p = plan.batch(rho0[:1], progs[:1], 0.0, DT_OUT, CPU_SAMPLES, F,
+                                   readout_weights=w, want_trace=True)
+        fl_ref = ref @ w
+        line["parity"] = {
+            "vs": "the reference's algorithm (CPU oracle, reference mode) on trajectory 0, "
+                  f"{CPU_SAMPLES} samples x F={F}",
+            "density_max_abs": float(np.abs(tr_p[0] - ref).max()),
+            "fluorescence_rel_max": float(np.abs(ro_p[0] - fl_ref).max()/np.abs(fl_ref).max()),
+            "bars": {"density_max_abs": 1e-10, "fluorescence_rel": 1e-9}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
