@@ -802,15 +802,22 @@ int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_pe
     if (per_sm < 1) return fail(SSS_EINVAL, "batched kernel does not fit on an SM");
     int want = (a.ntraj + slots_per_cta - 1) / slots_per_cta;
     int grid = std::max(1, std::min(want, per_sm * p->num_sms));
-    if (!p->ev_begin) {
+    // the launch's own timing events, except while the stream is being
+    // captured into a graph (events recorded there cannot be waited on)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    SSS_CUDA(cudaStreamIsCapturing(st, &cap));
+    const bool timed = cap == cudaStreamCaptureStatusNone;
+    if (timed && !p->ev_begin) {
         SSS_CUDA(cudaEventCreate(&p->ev_begin));
         SSS_CUDA(cudaEventCreate(&p->ev_end));
     }
-    SSS_CUDA(cudaEventRecord(p->ev_begin, st));
+    if (timed) SSS_CUDA(cudaEventRecord(p->ev_begin, st));
     kern<<<grid, threads, smem, st>>>(a);
     SSS_CUDA(cudaGetLastError());
-    SSS_CUDA(cudaEventRecord(p->ev_end, st));
-    p->ev_recorded = true;
+    if (timed) {
+        SSS_CUDA(cudaEventRecord(p->ev_end, st));
+        p->ev_recorded = true;
+    }
     p->last_grid = grid;
     return SSS_OK;
 }
