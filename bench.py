@@ -478,6 +478,7 @@ def main():
     kms = statistics.mean(kernel_ms) if not n_chunks else statistics.mean(times)
     achieved = fl*units_per_step/(kms*1e-3)/1e12
     peak = _lib.fp64_peak_tflops()
+    mma_peak = _lib.fp64_mma_peak_tflops()
     line = {"metric": METRIC, "value": value, "unit": "traj-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms/args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -509,6 +510,11 @@ def main():
                                          "(profiles/batch_odmr_nv7.md); inputs are read once, "
                                          "so it does not grow with the step count",
                          "peak_source": "measured live (sss_fp64_peak DFMA loop)",
+                         "fp64_tensor": {"dmma_peak": mma_peak, "unit": "TFLOP/s",
+                                         "used": False,
+                                         "note": "measured live (sss_fp64_mma_peak, mma.sync "
+                                                 "m8n8k4 f64); below the DFMA peak, so the "
+                                                 "sparse vector action stays on DFMA"},
                          "flops_per_traj_step": fl},
             "clocks": clock_info,
             "fluorescence_check": float(np.mean(fluor))}

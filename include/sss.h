@@ -256,6 +256,13 @@ int sss_plan_batch_info(const sss_plan* plan, int* lanes, int* degree,
  * denominator of the FP64-bound kernels. */
 int sss_fp64_peak(double* tflops, void* cuda_stream);
 
+/* Measurement utility (no reference counterpart): FP64 tensor-core (DMMA,
+ * mma.sync m8n8k4 f64) throughput in TFLOP/s from a bounded loop over 8
+ * independent accumulator tiles per warp, 4 CTAs of 256 threads per SM.
+ * Reported beside sss_fp64_peak: on GB300 it is below the DFMA rate, which
+ * is why no kernel here uses the FP64 tensor path. */
+int sss_fp64_mma_peak(double* tflops, void* cuda_stream);
+
 /* Allocation-free simulate for one trajectory (no counterpart in the
  * reference, which always allocates per call).  For callers that cannot
  * allocate device memory -- code inside another framework's memory pool, a

@@ -25,7 +25,7 @@ SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
            "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
            "sss_plan_set_projection", "sss_plan_set_unitary",
-           "sss_fp64_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
+           "sss_fp64_peak", "sss_fp64_mma_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
            "sss_batch_launch", "sss_last_error",
            "sss_plan_destroy"]
 
@@ -83,6 +83,8 @@ def load(build_if_missing=True):
         L.sss_plan_set_unitary.restype = i
         L.sss_plan_batch_info.argtypes = [vp, ip, ip, ip, ip, ip, dp]
         L.sss_fp64_peak.argtypes = [dp, vp]
+        L.sss_fp64_mma_peak.argtypes = [dp, vp]
+        L.sss_fp64_mma_peak.restype = i
         L.sss_adjoint_run.argtypes = [vp, i, vp, i, i, vp, d, d, i, i, dp, dp, vp, vp, i, vp]
         L.sss_adjoint_run.restype = i
         L.sss_batch_prepare.argtypes = [vp, i, vp, i, i, vp, d, i, dp, vp]
@@ -314,4 +316,11 @@ def fp64_peak_tflops(stream=None):
     """Measured FP64 FMA throughput of the current GPU (TFLOP/s)."""
     v = ctypes.c_double()
     check(load().sss_fp64_peak(ctypes.byref(v), stream))
+    return v.value
+
+
+def fp64_mma_peak_tflops(stream=None):
+    """Measured FP64 tensor-core (DMMA) throughput of the current GPU (TFLOP/s)."""
+    v = ctypes.c_double()
+    check(load().sss_fp64_mma_peak(ctypes.byref(v), stream))
     return v.value

@@ -470,6 +470,56 @@ int sss_fp64_peak(double* tflops, void* stream) {
     return SSS_OK;
 }
 
+// FP64 tensor-core (DMMA) throughput probe: mma.sync m8n8k4 f64 on 8
+// independent accumulator tiles per warp in a bounded loop.
+static __global__ void k_dmma_peak(double* out, int iters, double a, double b) {
+    double c[8][2];
+    for (int j = 0; j < 8; j++) {
+        c[j][0] = 0.0;
+        c[j][1] = 0.0;
+    }
+    const double x = a + threadIdx.x * 1e-12, y = b;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            asm volatile(
+                "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
+                : "+d"(c[j][0]), "+d"(c[j][1])
+                : "d"(x), "d"(y));
+    }
+    double s = 0.0;
+    for (int j = 0; j < 8; j++) s += c[j][0] + c[j][1];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int sss_fp64_mma_peak(double* tflops, void* stream) {
+    if (!tflops) return fail(SSS_EINVAL, "null output");
+    int dev = 0, sms = 0;
+    SSS_CUDA(cudaGetDevice(&dev));
+    SSS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int blocks = sms * 4, threads = 256, iters = 4096;
+    double* buf = nullptr;
+    SSS_CUDA(cudaMalloc(&buf, sizeof(double) * blocks * threads));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_dmma_peak<<<blocks, threads, 0, st>>>(buf, 128, 1e-3, 1e-3);
+    cudaEventRecord(e0, st);
+    k_dmma_peak<<<blocks, threads, 0, st>>>(buf, iters, 1e-3, 1e-3);
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, "fp64 tensor-core peak probe");
+    // 2*8*8*4 flop per warp-wide m8n8k4, 8 tiles per iteration
+    *tflops = 512.0 * 8 * iters * ((double)blocks * threads / 32) / (ms * 1e-3) / 1e12;
+    return SSS_OK;
+}
+
 int sss_plan_set_batch_config(sss_plan* p, int lanes, int cta_threads, int variant) {
     if (!p) return fail(SSS_EINVAL, "null plan");
     if (lanes < 0 || lanes > 256 || (lanes & (lanes - 1)))
