@@ -1,8 +1,8 @@
 """CPU oracle for the time-stepping hot path -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of
-``bench.py`` import this module, and only as the checker or the timed CPU
-baseline.  The product package never imports it.
+``bench.py`` import this module: to check the CUDA path's results, or as
+the timed CPU baseline.  The product package never imports it.
 
 It wraps ``sss_oracle.c`` (built by ``oracle/Makefile`` into
 ``oracle/_build/libsss_oracle.so``) and restates in numpy the host-side

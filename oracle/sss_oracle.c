@@ -2,8 +2,8 @@
  * sss_oracle.c -- CPU oracle for the time-stepping hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / reference legs of bench.py load this library, and only as
- * the checker or as the timed CPU baseline.  The product (superspinsim_gb300)
+ * cpu_baseline / reference legs of bench.py load this library: to check the
+ * CUDA path's results, or as the timed CPU baseline.  The product (superspinsim_gb300)
  * never calls it.
  *
  * It restates the CPU path of the reference's compiled simulator,

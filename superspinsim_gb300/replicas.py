@@ -20,7 +20,7 @@ def world():
 
 
 def init(backend=None):
-    """Initialise torch.distributed when WORLD_SIZE > 1 (nccl on GPU machines,
+    """Initialise torch.distributed when WORLD_SIZE > 1 (nccl with a GPU,
     gloo otherwise).  Returns (rank, world_size)."""
     rank, size = world()
     if size > 1:
