@@ -151,3 +151,35 @@ def test_batch_rotating_needs_row_parts():
     rho[1, 1] = 1
     with pytest.raises(_lib.SSSError, match="row-part"):
         sw.run(rho, progs, 0.0, 2e-9 + 1e-13, 1e-9, final_state=True)
+
+
+def test_batch_rotating_ragged_with_empty_trajectories():
+    """Ragged lengths including trajectories of zero samples, rotating frame:
+    the batched readouts and final states against the plain path on the same
+    rotating plan; an empty trajectory's final state is its initial state (to
+    the rounding of V V^-1) and its readout row stays zero."""
+    from superspinsim_gb300.sweep import Sweep
+    c = load_case("nv7_n49")
+    gens, vm = c["generators"], c["vectorisation_map"]
+    N = vm.shape[0]
+    rng = np.random.default_rng(8)
+    B, T, dt, F = 13, 5, 1e-9, 40
+    progs = _odmr_programs(F_RES + rng.uniform(-5e6, 5e6, B), 5e6/28.025e9, 10/65.9)
+    samples = rng.integers(0, T + 1, B).astype(np.int32)
+    samples[[0, 5]] = 0
+    rho = np.zeros((7, 7), complex)
+    rho[0, 0], rho[1, 1] = 0.4, 0.6
+    flat = np.stack([oracle.flatten(rho, vm, N)]*B)
+    w = _excited_weights(vm)
+    sw = Sweep(gens, vm, number_of_exponentials=2, number_of_fine_divisions=F,
+               use_rotating=True, time_step=dt)
+    ro, fin = sw.plan.batch(flat, progs, 0.0, dt, T, F, samples=samples, readout_weights=w,
+                            want_final=True)
+    full = sw.plan.simulate(flat, progs, 0.0, dt, T, F)   # plain path, same rotating plan
+    for b in range(B):
+        n = int(samples[b])
+        if n:
+            assert np.abs(ro[b, :n] - full[b, :n] @ w).max() <= 1e-12
+        assert np.all(ro[b, n:] == 0.0)
+        last = full[b, n - 1] if n else flat[b]
+        assert np.abs(fin[b] - last).max() <= 1e-12
