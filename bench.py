@@ -257,9 +257,10 @@ def run_reference_arm(args, rank, world):
             "ms_per_step": 1e3*total_time/args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "NV-7 ODMR sweep (bounded CPU sample)", "n_levels": 7,
-                       "liouvillian": "49x49", "method": "CF4:2", "dt_s": DT_OUT/F,
-                       "parallelism": "host cores"},
+            "config": {**build_workload("odmr", args)[-1], "frame": "lab", "method": "CF4:2",
+                       "dt_s": DT_OUT/F, "samples": int(round(args.duration/DT_OUT)),
+                       "fine_divisions": F, "parallelism": "host cores",
+                       "sample": cb["sample"]},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "traj-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
