@@ -568,7 +568,7 @@ void sss_plan_destroy(sss_plan* p) {
                       &p->w_prop, &p->w_in, &p->w_out, &p->w_prog, &p->w_tab, &p->w_aux,
                       &p->w_queue, &p->w_ro, &p->w_fin, &p->w_samples, &p->w_status,
                       &p->w_state, &p->w_adjf, &p->w_adjb, &p->w_states, &p->w_adjro,
-                      &p->w_adjst};
+                      &p->w_adjst, &p->w_order};
     for (DevBuf* b : bufs) b->release();
     if (p->ev_begin) cudaEventDestroy(p->ev_begin);
     if (p->ev_end) cudaEventDestroy(p->ev_end);

@@ -139,6 +139,7 @@ struct BatchArgs {
     const double* blk_self;    // M: e^{L0 h} diagonal coefficient of each row (minus 1 when residual)
     const double* blk_part;    // M: coefficient of its partner row
     const int* blk_pos;        // M: the partner's row (M: none, the zero row)
+    const int* order;          // ntraj: queue position -> trajectory (longest first), or null
     double* states;            // state before every exponential, or null:
     long st_steps;             //   [((b*st_steps + n)*K + e)*M + row], n = step since t_begin
     double inv_j[kMaxTaylor + 1];
@@ -217,6 +218,7 @@ __global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
             nb = __shfl_sync(gmask, nb, leader);
             b = nb;
             if (b >= a.ntraj) break;
+            if (a.order) b = __ldg(a.order + b);
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
@@ -349,6 +351,7 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
             nb = __shfl_sync(gmask, nb, leader);
             b = nb;
             if (b >= a.ntraj) break;
+            if (a.order) b = __ldg(a.order + b);
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
@@ -475,6 +478,7 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
             nb = __shfl_sync(gmask, nb, leader);
             b = nb;
             if (b >= a.ntraj) break;
+            if (a.order) b = __ldg(a.order + b);
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
             prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
@@ -659,6 +663,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             }
             b = nb;
             if (b >= a.ntraj) break;
+            if (a.order) b = __ldg(a.order + b);
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
             rp = kRing;
@@ -1580,7 +1585,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
 
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st, double* d_trace) {
+                 cudaStream_t st, double* d_trace, const int* d_order) {
     if (!p->batch_ready) return fail(SSS_EINVAL, "no prepared batch (call sss_batch_prepare)");
     p->last_launches = 0;
     if (p->batch_empty || n_samples <= 0) {
@@ -1597,6 +1602,7 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
     a.samples = d_samples;
     a.readout = d_readout;
     a.trace = d_trace;
+    a.order = d_order;
     a.rw = d_readout ? a.rw : nullptr;
     a.t0 = t0;
     a.t_begin = t_begin;
@@ -1691,8 +1697,26 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
               const int* d_samples, const int* h_samples, double t0, double dt, int T_max, int F,
               const double* h_rw, double* d_readout, double* d_final, cudaStream_t st,
               double* d_trace) {
-    (void)h_samples;
     const int N = p->d.N;
+    // uneven lengths: hand trajectories out longest first, so that the
+    // groups sharing a warp run for about as long and the queue balances
+    // the tail (longest-processing-time order)
+    const int* d_order = nullptr;
+    if (h_samples && ntraj > 1) {
+        std::vector<int> order(ntraj);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return h_samples[x] > h_samples[y]; });
+        bool identity = true;
+        for (int i = 0; i < ntraj && identity; i++) identity = order[i] == i;
+        if (!identity) {
+            if (int rc = p->w_order.ensure(sizeof(int) * (size_t)ntraj)) return rc;
+            SSS_CUDA(cudaMemcpyAsync(p->w_order.p, order.data(), sizeof(int) * (size_t)ntraj,
+                                     cudaMemcpyHostToDevice, st));
+            SSS_CUDA(cudaStreamSynchronize(st));  // the host order goes out of scope
+            d_order = p->w_order.as<int>();
+        }
+    }
     if (d_trace)
         SSS_CUDA(cudaMemsetAsync(d_trace, 0, sizeof(double) * (size_t)ntraj * T_max * N, st));
     if (int rc = batch_prepare(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, h_rw, st)) return rc;
@@ -1705,7 +1729,8 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     if (state != d_rho0)
         SSS_CUDA(cudaMemcpyAsync(state, d_rho0, sizeof(double) * (size_t)ntraj * N,
                                  cudaMemcpyDeviceToDevice, st));
-    return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st, d_trace);
+    return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st, d_trace,
+                        d_order);
 }
 
 }  // namespace sss

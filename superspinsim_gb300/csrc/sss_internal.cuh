@@ -118,7 +118,7 @@ struct sss_plan {
     sss::DevBuf w_state;
     // adjoint (row-part path): forward and backward tables, stored states,
     // readouts, state buffer
-    sss::DevBuf w_adjf, w_adjb, w_states, w_adjro, w_adjst;
+    sss::DevBuf w_adjf, w_adjb, w_states, w_adjro, w_adjst, w_order;
     size_t adj_max_bytes = 0;  // stored-state memory of the adjoint, 0: half the free memory
     // equivalence-class (kernel) mode: states of n_full entries, image basis P
     // (n_full x N); unitary mode: operator generators of a u_n-level system
@@ -152,7 +152,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
                   const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st);
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st, double* d_trace = nullptr);
+                 cudaStream_t st, double* d_trace = nullptr, const int* d_order = nullptr);
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
                  bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts = false);
