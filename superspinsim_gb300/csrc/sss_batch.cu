@@ -1225,7 +1225,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
             int chosen = 0;
             long parts4 = 0;  // parts of at most 4 entries: lanes beyond twice that stay idle
             for (const auto& re : Ly.row_ents) parts4 += std::max<long>(1, ((long)re.size() + 3) / 4);
-            for (int Lc : {16, 32, 64, 128, 256}) {
+            for (int Lc : {8, 16, 32, 64, 128, 256}) {
                 if (chosen && Lc > 2 * parts4) break;
                 BatchLayout trial;
                 trial.row_ents = Ly.row_ents;
