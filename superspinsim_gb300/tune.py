@@ -18,7 +18,8 @@ _CACHE = {}
 def _key(sweep, B, progs):
     g = sweep.generators
     active = tuple(bool(np.any(progs[:, c, :, 1:3] != 0)) for c in range(progs.shape[1]))
-    return (g.shape, float(np.abs(g).sum()), B, sweep.F, active)
+    frame = None if getattr(sweep, "rotating", None) is None else sweep.time_step
+    return (g.shape, float(np.abs(g).sum()), B, sweep.F, active, frame)
 
 
 def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, repeats=2,
