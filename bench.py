@@ -267,33 +267,30 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_adjoint_workload(args, rank, world):
-    """Adjoint gradients of integrated fluorescence for 256 seeded pulse
-    shapes (128 piecewise-constant segments of 2 ns, Rabi 0-20 MHz, phase
-    0-2pi, carrier at the ms=0 -> +1 line, B = 5 mT) followed by a 300 ns
-    laser readout: 556 ns = 111,200 steps at 5 ps per shape.  Times the
-    checkpointed adjoint (objective + 256 gradients per shape) against one
-    forward solve of the same batch."""
-    import torch
+def adjoint_workload(nv21=False, n_traj=0):
+    """Pulse-shape objective of the adjoint workloads: NV-7 at 5 mT, 256
+    seeded shapes of 128 piecewise-constant segments of 2 ns (Rabi 0-20 MHz,
+    phase 0-2pi, carrier at the ms=0 -> +1 line), or NV-21 (14N) at 50 mT,
+    32 shapes of 64 segments; each followed by a 300 ns laser readout whose
+    integrated fluorescence is the objective.  Returns (Objective, programs
+    (B,4,S,5), T, time weights, S, name)."""
     from superspinsim_gb300 import protocols
     from superspinsim_gb300.adjoint import Objective, trapezoid_weights
-    nv21 = args.workload == "adjoint-nv21"
     if nv21:
-        # NV-21 (14N) at 50 mT: 32 shapes of 64 segments
         from superspinsim_gb300 import models
         from superspinsim_gb300.generators import generate_atoms
         spins, inter, groups = models.nv_21(np.array([0.0, 0.0, 0.05]),
                                             params=models.nv21_params())
         g, vm = generate_atoms(spins, inter, groups, use_incoherent=False)
         gens = np.array([g["generators"][k] for k in ("L0", "Gx", "Gy", "Gz", "Gr")])
-        B, S, f_c = args.n_traj or 32, 64, 2.870e9 + GAMMA*0.05
+        B, S, f_c = n_traj or 32, 64, 2.870e9 + GAMMA*0.05
         rho = np.zeros((21, 21), complex)
         for k in range(3, 6):
             rho[k, k] = 1/3
         levels = list(range(9, 18))
     else:
         gens, vm = nv7_model()
-        B, S, f_c = args.n_traj or 256, 128, F_RES
+        B, S, f_c = n_traj or 256, 128, F_RES
         rho = np.zeros((7, 7), complex)
         rho[1, 1] = 1.0
         levels = [3, 4, 5]
@@ -305,6 +302,15 @@ def run_adjoint_workload(args, rank, world):
     tw = trapezoid_weights(T, DT_OUT, S*2 - 1, T - 1)
     obj = Objective(gens, vm, rho, levels, 65.9e6, number_of_exponentials=K_EXP,
                     number_of_fine_divisions=F)
+    return obj, progs, T, tw, S, "NV-21" if nv21 else "NV-7"
+
+
+def run_adjoint_workload(args, rank, world):
+    """Times the checkpointed adjoint (objective + 2S gradients per shape)
+    of adjoint_workload against one forward solve of the same batch."""
+    import torch
+    obj, progs, T, tw, S, name = adjoint_workload(args.workload == "adjoint-nv21", args.n_traj)
+    B = progs.shape[0]
     for _ in range(args.warmup):
         obj.run(progs, DT_OUT, T, tw)
     torch.cuda.synchronize()
@@ -318,7 +324,6 @@ def run_adjoint_workload(args, rank, world):
         adj.append(time.perf_counter() - t)
     fwd_s, adj_s = statistics.median(fwd), statistics.median(adj)
     steps = B*T*F
-    name = "NV-21" if nv21 else "NV-7"
     line = {"metric": f"{name} pulse-shape adjoint gradients/s", "value": B/adj_s,
             "unit": f"gradients/s ({2*S} parameters each)", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3*adj_s, "higher_is_better": True,
