@@ -147,6 +147,25 @@ int sss_batch_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                   double* final_state, double* trace, int host,
                   void* cuda_stream);
 
+/* sss_batch_run with sampled coefficients instead of programs: the
+ * fallback for arbitrary samplers (the reference's sampler callables,
+ * generate_simulator.py:235-271, evaluated by the caller).
+ *   coeff_table: ntraj*(F*T_max*Q)*G, per trajectory the rows of
+ *          sss_simulate's table with T = T_max: row (r*T_max + t)*Q + k
+ *          holds the G coefficients (lab [c_L0, c_1, ...], rotating
+ *          [c_1, ...]) at node k of fine step r of output sample t.
+ * Runs on the row-part kernel (variant 0 or 4).  A column that holds one
+ * value everywhere is folded into the constant part of Omega; the Taylor
+ * degree follows the table's largest |coefficient| per column.  NaN or
+ * infinity anywhere in the table is SSS_ENONFINITE.  The other arguments
+ * are sss_batch_run's. */
+int sss_batch_run_table(sss_plan* plan, int ntraj, const double* rho0,
+                        const double* coeff_table, const int* samples,
+                        double t0, double dt, int T_max, int F,
+                        const double* readout_weights, double* readout,
+                        double* final_state, double* trace, int host,
+                        void* cuda_stream);
+
 /* The batched run in two parts (no reference counterpart).
  * sss_batch_prepare analyses the batch on the host -- active generators,
  * rows reachable from rho0's support, lane layout, Taylor degree from the

@@ -22,7 +22,7 @@ ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
           -5: "ENONFINITE", -6: "ENODEVICE"}
 
 SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
-           "sss_simulate_device", "sss_batch_run", "sss_plan_last_launches",
+           "sss_simulate_device", "sss_batch_run", "sss_batch_run_table", "sss_plan_last_launches",
            "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
            "sss_plan_set_projection", "sss_plan_set_unitary",
            "sss_fp64_peak", "sss_fp64_mma_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
@@ -73,6 +73,7 @@ def load(build_if_missing=True):
         L.sss_simulate.argtypes = sim
         L.sss_simulate_device.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, vp, vp]
         L.sss_batch_run.argtypes = [vp, i, vp, i, i, vp, vp, d, d, i, i, dp, vp, vp, vp, i, vp]
+        L.sss_batch_run_table.argtypes = [vp, i, vp, vp, vp, d, d, i, i, dp, vp, vp, vp, i, vp]
         L.sss_plan_last_launches.argtypes = [vp]
         L.sss_plan_set_batch_config.argtypes = [vp, i, i, i]
         L.sss_plan_set_adjoint_memory.argtypes = [vp, ctypes.c_size_t]
@@ -222,26 +223,39 @@ class Plan:
         return out
 
     def batch(self, rho0, programs, t0, dt, T_max, F, samples=None,
-              readout_weights=None, want_final=False, stream=None, want_trace=False):
+              readout_weights=None, want_final=False, stream=None, want_trace=False,
+              table=None):
         """Host-buffer batched run.  Returns (readout (B, T_max) or None,
-        final (B, N) or None[, trace (B, T_max, N)])."""
+        final (B, N) or None[, trace (B, T_max, N)]).  `table` (B, F*T_max*Q,
+        G) -- sampled coefficients in sss_simulate's row order -- replaces
+        the programs (then None)."""
         rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
-        programs = np.ascontiguousarray(programs, dtype=np.float64)
         B = rho0.shape[0]
-        nch, nseg = programs.shape[1], programs.shape[2]
         ro = np.empty((B, T_max)) if readout_weights is not None else None
         fin = np.empty((B, self.N)) if want_final else None
         tr = np.empty((B, T_max, self.N)) if want_trace else None
         rw = None if readout_weights is None else np.ascontiguousarray(
             readout_weights, dtype=np.float64)
         smp = None if samples is None else np.ascontiguousarray(samples, dtype=np.int32)
-        check(load().sss_batch_run(
-            self._h, B, rho0.ctypes.data_as(ctypes.c_void_p), nch, nseg,
-            programs.ctypes.data_as(ctypes.c_void_p), iptr(smp), float(t0), float(dt),
-            int(T_max), int(F), dptr(rw),
-            None if ro is None else ro.ctypes.data_as(ctypes.c_void_p),
-            None if fin is None else fin.ctypes.data_as(ctypes.c_void_p),
-            None if tr is None else tr.ctypes.data_as(ctypes.c_void_p), 1, stream))
+        outs = (None if ro is None else ro.ctypes.data_as(ctypes.c_void_p),
+                None if fin is None else fin.ctypes.data_as(ctypes.c_void_p),
+                None if tr is None else tr.ctypes.data_as(ctypes.c_void_p))
+        if table is not None:
+            table = np.ascontiguousarray(table, dtype=np.float64)
+            if table.shape != (B, F*T_max*self.Q, self.G):
+                raise ValueError(f"coefficient table of shape {table.shape}, expected "
+                                 f"{(B, F*T_max*self.Q, self.G)}")
+            check(load().sss_batch_run_table(
+                self._h, B, rho0.ctypes.data_as(ctypes.c_void_p),
+                table.ctypes.data_as(ctypes.c_void_p), iptr(smp), float(t0), float(dt),
+                int(T_max), int(F), dptr(rw), *outs, 1, stream))
+        else:
+            programs = np.ascontiguousarray(programs, dtype=np.float64)
+            nch, nseg = programs.shape[1], programs.shape[2]
+            check(load().sss_batch_run(
+                self._h, B, rho0.ctypes.data_as(ctypes.c_void_p), nch, nseg,
+                programs.ctypes.data_as(ctypes.c_void_p), iptr(smp), float(t0), float(dt),
+                int(T_max), int(F), dptr(rw), *outs, 1, stream))
         if want_trace:
             return ro, fin, tr
         return ro, fin

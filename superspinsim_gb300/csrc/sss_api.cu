@@ -266,15 +266,22 @@ int sss_simulate_device(sss_plan* p, int ntraj, const double* rho0, int nch, int
     return simulate_impl(p, ntraj, rho0, nch, nseg, programs, tab, t0, dt, T, F, out, stream, false);
 }
 
-int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
-                  const double* programs, const int* samples, double t0, double dt, int T_max,
-                  int F, const double* readout_weights, double* readout, double* final_state,
-                  double* trace, int host, void* stream) {
-    if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, T_max, F,
+// sss_batch_run and sss_batch_run_table: programs, or a coefficient table
+static int batch_run_impl(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                          const double* programs, const double* tab, const int* samples, double t0,
+                          double dt, int T_max, int F, const double* readout_weights,
+                          double* readout, double* final_state, double* trace, int host,
+                          void* stream) {
+    if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, tab, dt, T_max, F,
                            readout ? (const void*)readout
                                    : (final_state ? (const void*)final_state : (const void*)trace)))
         return rc;
-    if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
+    if (!programs && !tab)
+        return fail(SSS_EINVAL, "batched runs need a coefficient program or table");
+    if (tab) {
+        nch = p->d.G;
+        nseg = 0;
+    }
     if (p->rotating && p->D + p->S == 0) return fail(SSS_EINVAL, "rotating tables not set");
     if (p->n_full || p->u_n)
         return fail(SSS_EINVAL, "batched runs support neither projected nor unitary plans");
@@ -297,20 +304,27 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
             if (h_samples[b] < 0 || h_samples[b] > T_max)
                 return fail(SSS_EINVAL, "samples[b] must lie in [0, T_max]");
     }
-    const double *d_rho0 = rho0, *d_prog = programs;
+    const double *d_rho0 = rho0, *d_prog = programs, *d_tab = tab;
     const int* d_samples = samples;
     double *d_ro = readout, *d_fin = final_state, *d_tr = trace;
-    size_t nprog = (size_t)ntraj * nch * nseg * 5;
+    const size_t nprog = tab ? 0 : (size_t)ntraj * nch * nseg * 5;
+    const size_t ntab = tab ? (size_t)ntraj * F * T_max * p->d.Q * p->d.G : 0;
     if (host) {
         for (size_t i = 0; i < nprog; i++)
             if (std::isnan(programs[i])) return fail(SSS_ENONFINITE, "program contains NaN");
-        if (int rc = p->w_in.ensure(sizeof(double) * ((size_t)ntraj * N + nprog))) return rc;
+        if (int rc = p->w_in.ensure(sizeof(double) * ((size_t)ntraj * N + nprog + ntab))) return rc;
         double* base = p->w_in.as<double>();
         SSS_CUDA(cudaMemcpyAsync(base, rho0, sizeof(double) * ntraj * N, cudaMemcpyHostToDevice, st));
-        SSS_CUDA(cudaMemcpyAsync(base + (size_t)ntraj * N, programs, sizeof(double) * nprog,
-                                 cudaMemcpyHostToDevice, st));
         d_rho0 = base;
-        d_prog = base + (size_t)ntraj * N;
+        if (tab) {
+            SSS_CUDA(cudaMemcpyAsync(base + (size_t)ntraj * N, tab, sizeof(double) * ntab,
+                                     cudaMemcpyHostToDevice, st));
+            d_tab = base + (size_t)ntraj * N;
+        } else {
+            SSS_CUDA(cudaMemcpyAsync(base + (size_t)ntraj * N, programs, sizeof(double) * nprog,
+                                     cudaMemcpyHostToDevice, st));
+            d_prog = base + (size_t)ntraj * N;
+        }
         if (samples) {
             if (int rc = p->w_samples.ensure(sizeof(int) * ntraj)) return rc;
             SSS_CUDA(cudaMemcpyAsync(p->w_samples.p, samples, sizeof(int) * ntraj,
@@ -338,9 +352,9 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
         SSS_CUDA(cudaMemcpy(h_rho0.data(), rho0, sizeof(double) * h_rho0.size(), cudaMemcpyDeviceToHost));
     }
     (void)h_rho0;
-    int rc = batch_run(p, ntraj, d_rho0, nch, nseg, d_prog, d_samples,
+    int rc = batch_run(p, ntraj, d_rho0, nch, nseg, tab ? nullptr : d_prog, d_samples,
                        samples ? h_samples.data() : nullptr, t0, dt, T_max, F, readout_weights,
-                       d_ro, d_fin, st, d_tr);
+                       d_ro, d_fin, st, d_tr, d_tab);
     if (rc) return rc;
     if (host) {
         if (readout)
@@ -355,6 +369,22 @@ int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
         SSS_CUDA(cudaStreamSynchronize(st));
     }
     return SSS_OK;
+}
+
+int sss_batch_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                  const double* programs, const int* samples, double t0, double dt, int T_max,
+                  int F, const double* readout_weights, double* readout, double* final_state,
+                  double* trace, int host, void* stream) {
+    return batch_run_impl(p, ntraj, rho0, nch, nseg, programs, nullptr, samples, t0, dt, T_max, F,
+                          readout_weights, readout, final_state, trace, host, stream);
+}
+
+int sss_batch_run_table(sss_plan* p, int ntraj, const double* rho0, const double* coeff_table,
+                        const int* samples, double t0, double dt, int T_max, int F,
+                        const double* readout_weights, double* readout, double* final_state,
+                        double* trace, int host, void* stream) {
+    return batch_run_impl(p, ntraj, rho0, 0, 0, nullptr, coeff_table, samples, t0, dt, T_max, F,
+                          readout_weights, readout, final_state, trace, host, stream);
 }
 
 int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,

@@ -140,6 +140,11 @@ struct BatchArgs {
     const double* blk_part;    // M: coefficient of its partner row
     const int* blk_pos;        // M: the partner's row (M: none, the zero row)
     const int* order;          // ntraj: queue position -> trajectory (longest first), or null
+    // coefficient table instead of programs (row-part kernel): per trajectory
+    // F*T_max*Q rows of tab_G values, row (r*T_max + t)*Q + k for node k of
+    // fine step r of output sample t; a slot's channel is its table column
+    const double* tab;
+    int tab_G;
     double* states;            // state before every exponential, or null:
     long st_steps;             //   [((b*st_steps + n)*K + e)*M + row], n = step since t_begin
     double inv_j[kMaxTaylor + 1];
@@ -667,7 +672,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
             t = a.t_begin;
             rp = kRing;
-            prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
+            prog = a.prog ? a.prog + (size_t)b * a.nch * a.nseg * 5 : nullptr;
             const double* r0b = a.rho0 + (size_t)b * a.N;
             if (a.rot) {
                 // eigenbasis coordinates x = V^-1 rho0 on the kept rows
@@ -684,16 +689,26 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             if (t >= T_b) continue;
         }
         if (rp == kRing) {
-            // node values of the live channels for fine steps (t, r) .. +kRing-1,
-            // node time ((t0 + (r*dt)/F) + dt*t) + (dt*node)/F, each op rounded
+            // node values of the live channels for fine steps (t, r) .. +kRing-1:
+            // the program at node time ((t0 + (r*dt)/F) + dt*t) + (dt*node)/F,
+            // each op rounded, or the table's row (steps past the last sample
+            // of the table read as zero; a trajectory never uses them)
             for (int i = li; i < kRing * Q * NC; i += L) {
                 const int s = i / (Q * NC), rem = i - s * Q * NC, k = rem / NC, ci = rem - k * NC;
                 const int rr = r + s, ts = t + rr / a.F, rs = rr % a.F;
-                const double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + rs)),
-                                                      __dmul_rn(a.dt, (double)ts)),
-                                            __ldg(a.noff + k));
                 const int ch = a.lch_chan[ci];
-                ringc[i] = ch < a.nch ? channel_value(prog, a.nseg, ch, tn) : 0.0;
+                double val = 0.0;
+                if (a.tab) {
+                    if (ts < a.T_max)
+                        val = __ldg(a.tab + (((size_t)b * a.F + rs) * a.T_max + ts) * (size_t)(Q * a.tab_G) +
+                                    (size_t)k * a.tab_G + ch);
+                } else if (ch < a.nch) {
+                    const double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + rs)),
+                                                          __dmul_rn(a.dt, (double)ts)),
+                                                __ldg(a.noff + k));
+                    val = channel_value(prog, a.nseg, ch, tn);
+                }
+                ringc[i] = val;
             }
             gsync();
             // CF weights: lab generators sum their channel over the nodes; a
@@ -1041,30 +1056,127 @@ int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::En
     return SSS_OK;
 }
 
+// Per column of a coefficient table (rows x G): the largest |value|, the
+// smallest and largest value, and a count of non-finite values; one partial
+// per CTA in out[(cta*G + g)*4 + {0,1,2,3}], reduced on the host.
+__global__ void __launch_bounds__(256) k_table_stats(const double* __restrict__ tab, size_t rows,
+                                                     int G, double* __restrict__ out) {
+    __shared__ double s_red[8][kMaxG][4];
+    double st[kMaxG][4];
+    for (int g = 0; g < kMaxG; g++) {
+        st[g][0] = 0.0;
+        st[g][1] = INFINITY;
+        st[g][2] = -INFINITY;
+        st[g][3] = 0.0;
+    }
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += (size_t)gridDim.x * blockDim.x)
+        for (int g = 0; g < G; g++) {
+            const double v = __ldg(tab + r * G + g);
+            if (!isfinite(v)) {
+                st[g][3] += 1.0;
+            } else {
+                st[g][0] = fmax(st[g][0], fabs(v));
+                st[g][1] = fmin(st[g][1], v);
+                st[g][2] = fmax(st[g][2], v);
+            }
+        }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int g = 0; g < G; g++)
+        for (int o = 16; o > 0; o >>= 1) {
+            st[g][0] = fmax(st[g][0], __shfl_xor_sync(0xffffffffu, st[g][0], o));
+            st[g][1] = fmin(st[g][1], __shfl_xor_sync(0xffffffffu, st[g][1], o));
+            st[g][2] = fmax(st[g][2], __shfl_xor_sync(0xffffffffu, st[g][2], o));
+            st[g][3] += __shfl_xor_sync(0xffffffffu, st[g][3], o);
+        }
+    if (lane == 0)
+        for (int g = 0; g < G; g++)
+            for (int j = 0; j < 4; j++) s_red[warp][g][j] = st[g][j];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            for (int g = 0; g < G; g++) {
+                s_red[0][g][0] = fmax(s_red[0][g][0], s_red[w][g][0]);
+                s_red[0][g][1] = fmin(s_red[0][g][1], s_red[w][g][1]);
+                s_red[0][g][2] = fmax(s_red[0][g][2], s_red[w][g][2]);
+                s_red[0][g][3] += s_red[w][g][3];
+            }
+        for (int g = 0; g < G; g++)
+            for (int j = 0; j < 4; j++) out[((size_t)blockIdx.x * G + g) * 4 + j] = s_red[0][g][j];
+    }
+}
+
+// Column statistics of a device coefficient table: the channels' bounds
+// and which channels hold one value everywhere (folded into the constant
+// part of Omega).  A NaN or infinite entry is an error.
+static int table_stats(sss_plan* p, const double* d_tab, size_t rows, int G, std::vector<double>& chmax,
+                       std::vector<double>& chval, std::vector<char>& chconst, cudaStream_t st) {
+    const int threads = 256;
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((rows + threads - 1) / threads,
+                                                                 (size_t)2 * p->num_sms));
+    if (int rc = p->w_status.ensure(sizeof(double) * (size_t)blocks * G * 4)) return rc;
+    k_table_stats<<<blocks, threads, 0, st>>>(d_tab, rows, G, p->w_status.as<double>());
+    SSS_CUDA(cudaGetLastError());
+    std::vector<double> part((size_t)blocks * G * 4);
+    SSS_CUDA(cudaMemcpyAsync(part.data(), p->w_status.p, sizeof(double) * part.size(),
+                             cudaMemcpyDeviceToHost, st));
+    SSS_CUDA(cudaStreamSynchronize(st));
+    for (int g = 0; g < G; g++) {
+        double mx = 0.0, lo = INFINITY, hi = -INFINITY, bad = 0.0;
+        for (int c = 0; c < blocks; c++) {
+            const double* q = &part[((size_t)c * G + g) * 4];
+            mx = std::max(mx, q[0]);
+            lo = std::min(lo, q[1]);
+            hi = std::max(hi, q[2]);
+            bad += q[3];
+        }
+        if (bad > 0.0)
+            return fail(SSS_ENONFINITE, "coefficient table column " + std::to_string(g) +
+                                            " contains NaN or infinity");
+        chmax[g] = mx;
+        chconst[g] = rows > 0 && lo == hi;
+        chval[g] = rows > 0 ? lo : 0.0;
+    }
+    return SSS_OK;
+}
+
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
-                 bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts) {
+                 bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts,
+                 const double* d_tab, int T_tab) {
     const int N = p->d.N;
     const bool rot = p->rotating;
+    const bool table = d_tab != nullptr;
     BatchLayout& Ly = *out;
     const SparseGenerators& sp = p->sparse;
     const int G = sp.G;  // generator slots: lab generators, or rotating (node, generator)
-    // program channel of a slot: lab slot g is driven by channel g-1 (slot 0,
-    // L0, has coefficient 1); rotating slot k*G0 + g by channel g
-    auto slot_chan = [&](int a) { return rot ? a % p->d.G : a - 1; };
+    // channel of a slot.  Programs: lab slot g is driven by channel g-1 (slot
+    // 0, L0, has coefficient 1); rotating slot k*G0 + g by channel g.  A
+    // coefficient table: the slot's column (lab g, rotating g of node k).
+    if (table) {
+        nch = p->d.G;
+        nseg = 0;
+    }
+    auto slot_chan = [&](int a) { return rot ? a % p->d.G : (table ? a : a - 1); };
     std::vector<double> h_rho0((size_t)ntraj * N), h_prog((size_t)ntraj * nch * nseg * 5);
     SSS_CUDA(cudaMemcpyAsync(h_rho0.data(), d_rho0, sizeof(double) * h_rho0.size(),
                              cudaMemcpyDeviceToHost, st));
-    SSS_CUDA(cudaMemcpyAsync(h_prog.data(), d_prog, sizeof(double) * h_prog.size(),
-                             cudaMemcpyDeviceToHost, st));
+    if (!h_prog.empty())
+        SSS_CUDA(cudaMemcpyAsync(h_prog.data(), d_prog, sizeof(double) * h_prog.size(),
+                                 cudaMemcpyDeviceToHost, st));
     SSS_CUDA(cudaStreamSynchronize(st));
     // ---- channels: largest |coefficient|, and whether the channel holds one
     // constant value for every trajectory at all times (every segment of
-    // zero amplitude with the same offset, the last one never ending): the
-    // row-part kernel folds those into the constant part of Omega ----
+    // zero amplitude with the same offset, the last one never ending; or
+    // one value in the whole table column): the row-part kernel folds those
+    // into the constant part of Omega ----
     std::vector<double> chmax(std::max(nch, 1), 0.0), chval(std::max(nch, 1), 0.0);
     std::vector<char> chconst(std::max(nch, 1), 0);
-    for (int c = 0; c < nch; c++) {
+    if (table) {
+        const size_t rows = (size_t)ntraj * F * T_tab * p->d.Q;
+        if (int rc = table_stats(p, d_tab, rows, nch, chmax, chval, chconst, st)) return rc;
+    }
+    for (int c = 0; c < nch && !table; c++) {
         bool ok = ntraj > 0 && nseg > 0;
         double val = 0.0;
         for (int b = 0; b < ntraj; b++) {
@@ -1212,7 +1324,10 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
     // (two trajectories per warp, fewer instructions per trajectory)
     if (rot && !force_parts && allow_register && p->batch_variant != 0 && p->batch_variant != 4)
         return fail(SSS_EINVAL, "the rotating frame runs on the row-part kernel (variant 0 or 4)");
-    if (force_parts || (allow_register && (rot || p->batch_variant == 4 || p->batch_variant == 0))) {
+    if (table && !force_parts && p->batch_variant != 0 && p->batch_variant != 4)
+        return fail(SSS_EINVAL, "a coefficient table runs on the row-part kernel (variant 0 or 4)");
+    if (force_parts || (allow_register && (rot || table || p->batch_variant == 4 ||
+                                           p->batch_variant == 0))) {
         // lanes: as configured, or the narrowest group (fewest instructions
         // per trajectory) that still gives every SM sub-partition a warp and
         // whose pattern fits; else the widest that fits
@@ -1246,7 +1361,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
             Ly.degree = degree;
             Ly.substeps = substeps;
         }
-        if (rc == SSS_OK || p->batch_variant == 4 || force_parts || rot) return rc;
+        if (rc == SSS_OK || p->batch_variant == 4 || force_parts || rot || table) return rc;
     }
     if (L > 32)
         return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part variant, "
@@ -1505,6 +1620,8 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
         a.blk_pos = di + o_bpos;
     }
     a.rho0 = nullptr; a.prog = nullptr; a.samples = nullptr;
+    a.tab = nullptr;
+    a.tab_G = p->d.G;
     a.readout = nullptr; a.fin = nullptr;
     a.queue = p->w_queue.as<int>();
     for (int j = 0; j <= kMaxTaylor; j++) a.inv_j[j] = j ? 1.0 / j : 0.0;
@@ -1530,11 +1647,19 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
 }
 
 int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
-                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st) {
+                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st,
+                  const double* d_tab, int T_tab) {
     p->batch_ready = false;
     p->batch_empty = false;
+    if (d_tab) {
+        nch = p->d.G;
+        nseg = 0;
+    }
+    p->batch_table = d_tab != nullptr;
     BatchLayout Ly;
-    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st)) return rc;
+    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st, false,
+                              d_tab, T_tab))
+        return rc;
     if (Ly.M == 0) {
         p->batch_ready = true;
         p->batch_empty = true;
@@ -1585,8 +1710,11 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
 
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st, double* d_trace, const int* d_order) {
+                 cudaStream_t st, double* d_trace, const int* d_order, const double* d_tab) {
     if (!p->batch_ready) return fail(SSS_EINVAL, "no prepared batch (call sss_batch_prepare)");
+    if (p->batch_table != (d_tab != nullptr))
+        return fail(SSS_EINVAL, p->batch_table ? "the prepared batch runs from a coefficient table"
+                                               : "the prepared batch runs from programs");
     p->last_launches = 0;
     if (p->batch_empty || n_samples <= 0) {
         if (d_readout && n_samples > 0)
@@ -1603,6 +1731,7 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
     a.readout = d_readout;
     a.trace = d_trace;
     a.order = d_order;
+    a.tab = d_tab;
     a.rw = d_readout ? a.rw : nullptr;
     a.t0 = t0;
     a.t_begin = t_begin;
@@ -1696,7 +1825,7 @@ int parts_forward_launch(sss_plan* p, const PartsForward& fw, int ntraj, double*
 int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,
               const int* d_samples, const int* h_samples, double t0, double dt, int T_max, int F,
               const double* h_rw, double* d_readout, double* d_final, cudaStream_t st,
-              double* d_trace) {
+              double* d_trace, const double* d_tab) {
     const int N = p->d.N;
     // uneven lengths: hand trajectories out longest first, so that the
     // groups sharing a warp run for about as long and the queue balances
@@ -1719,7 +1848,8 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     }
     if (d_trace)
         SSS_CUDA(cudaMemsetAsync(d_trace, 0, sizeof(double) * (size_t)ntraj * T_max * N, st));
-    if (int rc = batch_prepare(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, h_rw, st)) return rc;
+    if (int rc = batch_prepare(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, h_rw, st, d_tab, T_max))
+        return rc;
     // the launch runs in place on a state buffer that starts as rho0
     double* state = d_final;
     if (!state) {
@@ -1730,7 +1860,7 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
         SSS_CUDA(cudaMemcpyAsync(state, d_rho0, sizeof(double) * (size_t)ntraj * N,
                                  cudaMemcpyDeviceToDevice, st));
     return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st, d_trace,
-                        d_order);
+                        d_order, d_tab);
 }
 
 }  // namespace sss

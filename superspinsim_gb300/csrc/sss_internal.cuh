@@ -109,7 +109,8 @@ struct sss_plan {
     // prepared batch (sss_batch_prepare -> sss_batch_launch)
     alignas(16) unsigned char batch_args[1024];
     bool batch_ready = false, batch_empty = false, batch_use_reg = false,
-         batch_one_chain = false, batch_has_rw = false, batch_parts = false;
+         batch_one_chain = false, batch_has_rw = false, batch_parts = false,
+         batch_table = false;
     int batch_C = 0, batch_P = 0;
     int batch_L = 0, batch_epl = 0, batch_threads_used = 0, batch_ntraj = 0, batch_nch = 0,
         batch_nseg = 0, batch_F = 0;
@@ -142,20 +143,26 @@ int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
 int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
               const double* d_prog, const int* d_samples, const int* h_samples,
               double t0, double dt, int T_max, int F, const double* h_rw,
-              double* d_readout, double* d_final, cudaStream_t st, double* d_trace = nullptr);
+              double* d_readout, double* d_final, cudaStream_t st, double* d_trace = nullptr,
+              const double* d_tab = nullptr);
 int build_sparse(sss_plan* p);
 // sss_adjoint.cu
 int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 const double* d_prog, double t0, double dt, int T, int F, const double* h_rw,
                 const double* h_tw, double* d_J, double* d_grad, cudaStream_t st);
+// d_tab: a coefficient table (ntraj*(F*T_tab*Q)*G, rows (r*T_tab + t)*Q + k)
+// in place of the programs; it runs on the row-part kernel
 int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
-                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st);
+                  const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st,
+                  const double* d_tab = nullptr, int T_tab = 0);
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st, double* d_trace = nullptr, const int* d_order = nullptr);
+                 cudaStream_t st, double* d_trace = nullptr, const int* d_order = nullptr,
+                 const double* d_tab = nullptr);
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
-                 bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts = false);
+                 bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts = false,
+                 const double* d_tab = nullptr, int T_tab = 0);
 int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows,
                       const std::vector<std::vector<char>>& prio, int L, int threads, int w_chain,
                       int w_close, const std::vector<int>& active,

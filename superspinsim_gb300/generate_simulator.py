@@ -240,16 +240,20 @@ def generate_simulator(
         if N > PLAIN_MAX_N:
             # larger than the dense shared-memory propagator path: the same
             # integrator through the batched kernel, full state per sample
+            # (a callable sampler is sampled on the host into a coefficient
+            # table, as for the dense path)
             if expm != "taylor":
                 raise NotImplementedError(
                     f"N = {N} > {PLAIN_MAX_N}: only expm='taylor' is supported at this size")
-            if not isinstance(sampler, (Program, np.ndarray)):
-                raise NotImplementedError(
-                    f"N = {N} > {PLAIN_MAX_N}: pass the coefficients as a Program")
-            prog = sampler.as_array() if isinstance(sampler, Program) else sampler
             plan = plan_for(time_step/F)
-            _, _, tr = plan.batch(flat0, prog[None], time_start, time_step, T, F,
-                                  want_trace=True)
+            if isinstance(sampler, (Program, np.ndarray)):
+                prog = sampler.as_array() if isinstance(sampler, Program) else sampler
+                _, _, tr = plan.batch(flat0, prog[None], time_start, time_step, T, F,
+                                      want_trace=True)
+            else:
+                tab = sample_table(sampler, G, time_start, time_step, T, F, nodes)
+                _, _, tr = plan.batch(flat0, None, time_start, time_step, T, F,
+                                      want_trace=True, table=tab)
             return time, unflatten_density(tr[0], n, vmap)
         plan = plan_for(time_step/F)
         if isinstance(sampler, Program):

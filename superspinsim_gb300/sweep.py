@@ -92,26 +92,46 @@ class Sweep:
     def run(self, rho0, programs, time_start, time_end, time_step, samples=None,
             readout_weights=None, final_state=False):
         """rho0: (B, n, n) complex or (B, N) flattened; programs: list of
-        Program or (B, 4, S, 5).  Returns dict with 'time' (T,), 'readout'
-        (B, T) and 'final' (B, N) as requested."""
-        progs = stack(programs) if isinstance(programs, (list, tuple)) and \
-            programs and isinstance(programs[0], Program) else \
-            np.ascontiguousarray(programs, dtype=np.float64)
-        flat = self.flatten(rho0)
-        if flat.shape[0] == 1 and progs.shape[0] > 1:
-            flat = np.repeat(flat, progs.shape[0], axis=0)
+        Program, (B, 4, S, 5), or a list of sampler callables
+        ``sampler(time, row)`` (the reference's form, sampled on the host
+        into a coefficient table).  Returns dict with 'time' (T,),
+        'readout' (B, T) and 'final' (B, N) as requested."""
         T = number_of_samples(time_start, time_end, time_step)
+        table = None
+        if isinstance(programs, (list, tuple)) and programs and callable(programs[0]) \
+                and not isinstance(programs[0], Program):
+            table = self.sample(programs, time_start, time_step, T)
+            progs = None
+            B = table.shape[0]
+        else:
+            progs = stack(programs) if isinstance(programs, (list, tuple)) and \
+                programs and isinstance(programs[0], Program) else \
+                np.ascontiguousarray(programs, dtype=np.float64)
+            B = progs.shape[0]
+        flat = self.flatten(rho0)
+        if flat.shape[0] == 1 and B > 1:
+            flat = np.repeat(flat, B, axis=0)
         if self.rotating is not None and time_step != self.time_step:
             self._make_plan(time_step)
         ro, fin = self.plan.batch(flat, progs, time_start, time_step, T, self.F,
                                   samples=samples, readout_weights=readout_weights,
-                                  want_final=final_state)
+                                  want_final=final_state, table=table)
         out = {"time": time_start + time_step*(np.arange(T) + 1)}
         if ro is not None:
             out["readout"] = ro
         if fin is not None:
             out["final"] = fin
         return out
+
+    def sample(self, samplers, time_start, time_step, T):
+        """Coefficient tables (B, F*T*Q, G) of sampler callables, one per
+        trajectory, in the row order of the batched table run (fine step
+        r, sample t, node k): lab rows [c_L0, c_1, ...] (the reference's
+        samplers write 1 for L0), rotating rows [c_1, ...]."""
+        from superspinsim_gb300.generate_simulator import sample_table
+        G = self.plan.G
+        return np.concatenate([sample_table(s, G, time_start, time_step, T, self.F, self.nodes)
+                               for s in samplers])
 
     def info(self):
         return self.plan.batch_info()
