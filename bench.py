@@ -499,7 +499,10 @@ def main():
                            "trials": len(tuned["trials"])},
                        "kernel": {"lanes": info["lanes"], "taylor_degree": info["degree"],
                                   "substeps": info["substeps"], "rows": info["rows"],
-                                  "nnz": info["nnz"]},
+                                  "nnz": info["nnz"],
+                                  # uneven lengths run in phases of widening lane
+                                  # groups; "lanes" is the last phase's
+                                  "launches_per_run": n_chunks or plan.last_launches()},
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "traj-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -831,7 +831,7 @@ int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_pe
         SSS_CUDA(cudaEventCreate(&p->ev_begin));
         SSS_CUDA(cudaEventCreate(&p->ev_end));
     }
-    if (timed) SSS_CUDA(cudaEventRecord(p->ev_begin, st));
+    if (timed && !p->ev_keep_begin) SSS_CUDA(cudaEventRecord(p->ev_begin, st));
     kern<<<grid, threads, smem, st>>>(a);
     SSS_CUDA(cudaGetLastError());
     if (timed) {
@@ -1348,7 +1348,8 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
                                       rows_reached, &trial, nullptr) != SSS_OK)
                     continue;
                 chosen = Lc;
-                if ((long)ntraj * Lc >= 4L * 32 * p->num_sms) break;
+                const long n_rule = p->auto_lanes_ntraj > 0 ? p->auto_lanes_ntraj : ntraj;
+                if (n_rule * Lc >= 4L * 32 * p->num_sms) break;
             }
             if (chosen)
                 rc = parts_layout_rows(p, Ly.row_ents, {}, chosen, threads_cfg, 1, 1, active,
@@ -1848,9 +1849,7 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     }
     if (d_trace)
         SSS_CUDA(cudaMemsetAsync(d_trace, 0, sizeof(double) * (size_t)ntraj * T_max * N, st));
-    if (int rc = batch_prepare(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, h_rw, st, d_tab, T_max))
-        return rc;
-    // the launch runs in place on a state buffer that starts as rho0
+    // the launches run in place on a state buffer that starts as rho0
     double* state = d_final;
     if (!state) {
         if (int rc = p->w_state.ensure(sizeof(double) * (size_t)ntraj * N)) return rc;
@@ -1859,8 +1858,51 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     if (state != d_rho0)
         SSS_CUDA(cudaMemcpyAsync(state, d_rho0, sizeof(double) * (size_t)ntraj * N,
                                  cudaMemcpyDeviceToDevice, st));
-    return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st, d_trace,
-                        d_order, d_tab);
+    // Uneven lengths with automatic lanes run in phases.  The automatic lane
+    // count is the narrowest group that still gives every SM sub-partition a
+    // warp; as trajectories finish, fewer groups remain, whole sub-partitions
+    // idle and the longest trajectories run at the speed of one narrow group.
+    // So the run stops where the trajectories still running no longer meet
+    // the lane rule and the rest is prepared again (from the current states)
+    // with the lane count the remaining trajectories call for: wider groups,
+    // shorter chains per trajectory.  Finished trajectories stay in the queue
+    // (they only pad their readout rows).  A phase ends on an output sample,
+    // as a chunked run does.
+    std::vector<int> longest;  // sample counts, longest first
+    const bool phased = h_samples && ntraj > 1 && p->batch_lanes == 0 &&
+                        (p->batch_variant == 0 || p->batch_variant == 4);
+    if (phased) {
+        longest.assign(h_samples, h_samples + ntraj);
+        std::sort(longest.begin(), longest.end(), std::greater<int>());
+    }
+    const double* prep_src = d_rho0;
+    int t = 0, launches = 0, prev_L = 0;
+    int rc = SSS_OK;
+    while (rc == SSS_OK && t < T_max) {
+        if (phased)
+            p->auto_lanes_ntraj = std::max<int>(
+                1, (int)(std::lower_bound(longest.begin(), longest.end(), t, std::greater<int>()) -
+                         longest.begin()));  // trajectories with more than t samples
+        rc = batch_prepare(p, ntraj, prep_src, nch, nseg, d_prog, dt, F, h_rw, st, d_tab, T_max);
+        p->auto_lanes_ntraj = 0;
+        if (rc) break;
+        int t_end = T_max;
+        if (phased && p->batch_parts && !p->batch_empty && p->batch_L > prev_L && launches < 8) {
+            // the lane rule holds while n * L >= 4*32*SMs trajectories' lanes
+            const long thr = (4L * 32 * p->num_sms + p->batch_L - 1) / p->batch_L;
+            if (thr <= ntraj && longest[thr - 1] > t) t_end = std::min(T_max, longest[thr - 1]);
+        }
+        prev_L = p->batch_L;
+        p->ev_keep_begin = launches > 0;
+        rc = batch_launch(p, state, d_prog, d_samples, t0, t, t_end - t, T_max, d_readout, st,
+                          d_trace, d_order, d_tab);
+        p->ev_keep_begin = false;
+        launches += p->last_launches;
+        prep_src = state;
+        t = t_end;
+    }
+    p->last_launches = launches;
+    return rc;
 }
 
 }  // namespace sss

@@ -104,8 +104,10 @@ struct sss_plan {
                             // 3: one-chain register variant, 4: row-part variant
     int device = 0;
     int num_sms = 0;
-    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // around the last batched kernel
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;  // around the last batched run's kernels
     bool ev_recorded = false;
+    bool ev_keep_begin = false;  // a later phase of one run: keep the first launch's begin event
+    int auto_lanes_ntraj = 0;    // trajectories the automatic lane rule counts (0: the batch)
     // prepared batch (sss_batch_prepare -> sss_batch_launch)
     alignas(16) unsigned char batch_args[1024];
     bool batch_ready = false, batch_empty = false, batch_use_reg = false,
