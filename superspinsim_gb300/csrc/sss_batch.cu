@@ -820,7 +820,13 @@ int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_pe
     int per_sm = 0;
     SSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
     if (per_sm < 1) return fail(SSS_EINVAL, "batched kernel does not fit on an SM");
-    int want = (a.ntraj + slots_per_cta - 1) / slots_per_cta;
+    // one group per trajectory with work in this launch (at most as many as
+    // fit): every group then starts on a trajectory of its own and the CTAs
+    // spread evenly over the SMs (a grid sized for trajectories that only
+    // pad their readout would leave the working ones wherever the queue
+    // happened to hand them out)
+    const int n_work = p->launch_active > 0 ? std::min(p->launch_active, a.ntraj) : a.ntraj;
+    int want = (n_work + slots_per_cta - 1) / slots_per_cta;
     int grid = std::max(1, std::min(want, per_sm * p->num_sms));
     // the launch's own timing events, except while the stream is being
     // captured into a graph (events recorded there cannot be waited on)
@@ -1879,10 +1885,14 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     int t = 0, launches = 0, prev_L = 0;
     int rc = SSS_OK;
     while (rc == SSS_OK && t < T_max) {
-        if (phased)
-            p->auto_lanes_ntraj = std::max<int>(
-                1, (int)(std::lower_bound(longest.begin(), longest.end(), t, std::greater<int>()) -
-                         longest.begin()));  // trajectories with more than t samples
+        // trajectories with more than t samples: the lane rule's count and
+        // the groups the launch needs (0: the whole batch)
+        const int n_running =
+            phased ? std::max<int>(1, (int)(std::lower_bound(longest.begin(), longest.end(), t,
+                                                             std::greater<int>()) -
+                                            longest.begin()))
+                   : 0;
+        p->auto_lanes_ntraj = n_running;
         rc = batch_prepare(p, ntraj, prep_src, nch, nseg, d_prog, dt, F, h_rw, st, d_tab, T_max);
         p->auto_lanes_ntraj = 0;
         if (rc) break;
@@ -1894,9 +1904,11 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
         }
         prev_L = p->batch_L;
         p->ev_keep_begin = launches > 0;
+        p->launch_active = n_running;
         rc = batch_launch(p, state, d_prog, d_samples, t0, t, t_end - t, T_max, d_readout, st,
                           d_trace, d_order, d_tab);
         p->ev_keep_begin = false;
+        p->launch_active = 0;
         launches += p->last_launches;
         prep_src = state;
         t = t_end;

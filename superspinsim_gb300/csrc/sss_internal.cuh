@@ -108,6 +108,7 @@ struct sss_plan {
     bool ev_recorded = false;
     bool ev_keep_begin = false;  // a later phase of one run: keep the first launch's begin event
     int auto_lanes_ntraj = 0;    // trajectories the automatic lane rule counts (0: the batch)
+    int launch_active = 0;       // trajectories with work in the next launch (0: the batch)
     // prepared batch (sss_batch_prepare -> sss_batch_launch)
     alignas(16) unsigned char batch_args[1024];
     bool batch_ready = false, batch_empty = false, batch_use_reg = false,
