@@ -236,6 +236,14 @@ def cases():
         dict(name="qubit_couple_rot_e1_nores", csv="qubit-couple",
              spins=QUBIT, ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0,
              t=(0, 10e-9, 1e-9), rot=True, res=False, K=1, F=10),
+        # the reference's test qubit-couple-res-rot-nh.py: the complex
+        # (non-Hermitian) basis, N = 2 n^2, no vectorisation map
+        dict(name="qubit_couple_rot_nh", csv="qubit-couple", spins=QUBIT,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0, t=(0, 10e-9, 1e-9),
+             rot=True, res=True, K=1, F=100, herm=False),
+        dict(name="qubit_couple_nh", csv="qubit-couple", spins=QUBIT,
+             ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0, t=(0, 10e-9, 1e-9),
+             rot=False, res=True, K=2, F=10, herm=False),
         dict(name="spin1_c1", csv=None, spins=spin1_c1(),
              ch=[c1_drive, ZERO, ZERO, ZERO], rho0=rho_c1,
              t=(0, 1e-9, 1e-9), rot=False, res=True, K=2, F=100,
@@ -388,7 +396,7 @@ def build_generators(c):
         make_rotating
     g, vmap = generate_atoms(
         c["spins"], c["spin_interactions"], c["group_interactions"],
-        False, True, c["use_incoherent"])
+        False, c.get("herm", True), c["use_incoherent"])
     gens = [g["generators"][k] for k in ["L0", "Gx", "Gy", "Gz", "Gr"]]
     out = dict(generators=np.array(gens), vectorisation_map=vmap)
     if c["rot"]:
@@ -410,8 +418,8 @@ def run_reference(c, K=None):
         number_of_fine_divisions=c["F"],
         number_of_quadratic_repeats=c["R"], use_rotating=c["rot"],
         use_residual=c["res"], use_kernel=False, use_unitary=False,
-        use_cuda=(c.get("path", "gpu") == "gpu"), use_hermitian=True,
-        use_incoherent=c["use_incoherent"])
+        use_cuda=(c.get("path", "gpu") == "gpu"),
+        use_hermitian=c.get("herm", True), use_incoherent=c["use_incoherent"])
     return dens
 
 
@@ -427,7 +435,7 @@ def save_case(c, extra_runs=()):
     arrays["rho0"] = c["rho0"]
     meta = dict(rot=c["rot"], res=c["res"], K=c["K"], F=c["F"], R=c["R"],
                 use_incoherent=c["use_incoherent"],
-                path=c.get("path", "gpu"))
+                path=c.get("path", "gpu"), herm=c.get("herm", True))
     if c["t"] is not None:
         arrays["times"] = np.array(c["t"], dtype=float)
         arrays["density"] = run_reference(c)

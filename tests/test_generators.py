@@ -20,7 +20,8 @@ LABELS = ["L0", "Gx", "Gy", "Gz", "Gr"]
 def test_generators_match_reference(c):
     z = load_case(c["name"])
     g, vm = generate_atoms(c["spins"], c["spin_interactions"], c["group_interactions"],
-                           use_incoherent=c["use_incoherent"])
+                           use_incoherent=c["use_incoherent"],
+                           use_hermitian=c.get("herm", True))
     gens = np.array([g["generators"][k] for k in LABELS])
     assert np.array_equal(vm, z["vectorisation_map"])
     ref = z["generators"]

@@ -30,15 +30,16 @@ def _excited_weights(vmap):
 
 
 @pytest.mark.parametrize("name", ["qubit_couple_rot_e5", "qubit_couple_rot_e1_nores",
-                                  "qubit_hyperfine"])
+                                  "qubit_hyperfine", "qubit_couple_rot_nh"])
 def test_batch_rotating_matches_reference_output(name):
     """Reference runs in the rotating frame (CF6:5 and CF2:1, residual and
-    plain arithmetic, a hyperfine pair): the batched kernel's full-state
-    trace against the reference's densities."""
+    plain arithmetic, a hyperfine pair, the complex non-Hermitian basis):
+    the batched kernel's full-state trace against the reference's
+    densities."""
     from superspinsim_gb300.generate_simulator import number_of_samples, unflatten_density
     from superspinsim_gb300.sweep import Sweep
     c = load_case(name)
-    vm = c["vectorisation_map"]
+    vm = c["vectorisation_map"] if bool(c.get("meta_herm", True)) else None
     K, F, res = int(c["meta_K"]), int(c["meta_F"]), bool(c["meta_res"])
     t0, tf, dt = (float(v) for v in c["times"])
     T = number_of_samples(t0, tf, dt)

@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 CASES = ["qubit_couple_res_e2", "qubit_couple_res_e5", "qubit_couple_res_e3_e6",
          "qubit_t1_0K", "qubit_t1_mK", "qutrit_couple", "qutrit_couple_unital",
          "qubit_hyperfine", "qubit_couple_rot_e5", "spin1_c1", "nv7_n49",
-         "nv7_n19"]
+         "nv7_n19", "qubit_couple_nh", "qubit_couple_rot_nh"]
 NONRES = ["qubit_couple", "qubit_couple_rot_e1_nores"]
 
 
@@ -27,8 +27,9 @@ def _sim(c, expm, K=None, T=None, dt=None, F=None):
         gens = c["generators_rotating"]
     else:
         gens = c["generators"]
+    herm = bool(c.get("meta_herm", True))
     sim = generate_simulator(
-        c["program"], gens, c["vectorisation_map"],
+        c["program"], gens, c["vectorisation_map"] if herm else None, use_hermitian=herm,
         use_residual=bool(c["meta_res"]), number_of_quartic_repeats=int(c["meta_R"]),
         number_of_exponentials=K, number_of_fine_divisions=F or int(c["meta_F"]),
         expm=expm, **kw)
@@ -68,7 +69,8 @@ def test_non_residual_reference_arithmetic(name):
 @pytest.mark.parametrize("name,T,dt,F", [("spin1_c1", 30, 1e-9, 100),
                                          ("nv7_n49", 3, 1e-9, 200),
                                          ("nv7_n19", 6, 1e-9, 200),
-                                         ("qubit_hyperfine", 40, 1e-9, 100)])
+                                         ("qubit_hyperfine", 40, 1e-9, 100),
+                                         ("qubit_couple_rot_nh", 40, 1e-9, 100)])
 def test_longer_window_against_oracle(name, T, dt, F):
     c = load_case(name)
     K = int(c["meta_K"])
@@ -81,7 +83,8 @@ def test_longer_window_against_oracle(name, T, dt, F):
     _, ref = oracle.simulate(c["generators"], c["rho0"], 0.0, T*dt + dt*1e-4, dt,
                              c["program"], K=K, W=W, nodes=nodes, F=F,
                              residual=bool(c["meta_res"]),
-                             vectorisation_map=c["vectorisation_map"], rotating=rot,
+                             vectorisation_map=c["vectorisation_map"]
+                             if bool(c.get("meta_herm", True)) else None, rotating=rot,
                              mode="vector", degree=16)
     _, d = _sim(c, "taylor", T=T, dt=dt, F=F)
     assert np.abs(d - ref).max() <= 1e-11
@@ -132,7 +135,8 @@ def _case_by_name(name):
 
 
 @pytest.mark.parametrize("name", ["qubit_couple_res_e2", "qubit_t1_mK", "qutrit_couple",
-                                  "qubit_hyperfine", "qubit_couple_rot_e5", "spin1_c1"])
+                                  "qubit_hyperfine", "qubit_couple_rot_e5", "spin1_c1",
+                                  "qubit_couple_rot_nh"])
 def test_simspins_front_end_matches_reference(name):
     """The whole front end -- this package's generator builder, rotating
     frame and simulator -- against the reference's simspins output."""
@@ -145,7 +149,7 @@ def test_simspins_front_end_matches_reference(name):
                     c["group_interactions"], c["rho0"], number_of_exponentials=c["K"],
                     number_of_fine_divisions=c["F"], number_of_quadratic_repeats=c["R"],
                     use_rotating=c["rot"], use_residual=c["res"],
-                    use_incoherent=c["use_incoherent"])
+                    use_incoherent=c["use_incoherent"], use_hermitian=c.get("herm", True))
     assert np.abs(d - ref["density"]).max() <= 1e-12
 
 
