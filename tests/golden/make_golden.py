@@ -236,6 +236,14 @@ def cases():
         dict(name="qubit_couple_rot_e1_nores", csv="qubit-couple",
              spins=QUBIT, ch=[q_drive, ZERO, ZERO, ZERO], rho0=rho_q0,
              t=(0, 10e-9, 1e-9), rot=True, res=False, K=1, F=10),
+        # the reference's qubit-t1-0K-res-rot.py and qubit-t1-mK-res-rot-e2.py:
+        # the rotating frame with decay (damped e^{L0 h} blocks)
+        dict(name="qubit_t1_0K_rot", csv=None, spins=qubit_t1(0),
+             ch=[drive(28e6, 10e-3, t_end=T1_END), ZERO, ZERO, ZERO],
+             rho0=rho_q1, t=(0, 20e-9, 1e-9), rot=True, res=True, K=1, F=100),
+        dict(name="qubit_t1_mK_rot_e2", csv=None, spins=qubit_t1(1e-3),
+             ch=[drive(28e6, 10e-3, t_end=T1_END), ZERO, ZERO, ZERO],
+             rho0=rho_q1, t=(0, 20e-9, 1e-9), rot=True, res=True, K=2, F=100),
         # the reference's test qubit-couple-res-rot-nh.py: the complex
         # (non-Hermitian) basis, N = 2 n^2, no vectorisation map
         dict(name="qubit_couple_rot_nh", csv="qubit-couple", spins=QUBIT,

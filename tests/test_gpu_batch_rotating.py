@@ -30,10 +30,12 @@ def _excited_weights(vmap):
 
 
 @pytest.mark.parametrize("name", ["qubit_couple_rot_e5", "qubit_couple_rot_e1_nores",
-                                  "qubit_hyperfine", "qubit_couple_rot_nh"])
+                                  "qubit_hyperfine", "qubit_couple_rot_nh", "qubit_t1_0K_rot",
+                                  "qubit_t1_mK_rot_e2"])
 def test_batch_rotating_matches_reference_output(name):
     """Reference runs in the rotating frame (CF6:5 and CF2:1, residual and
-    plain arithmetic, a hyperfine pair, the complex non-Hermitian basis):
+    plain arithmetic, a hyperfine pair, the complex non-Hermitian basis,
+    decay -- damped e^{L0 h} blocks -- at K = 1 and 2):
     the batched kernel's full-state trace against the reference's
     densities."""
     from superspinsim_gb300.generate_simulator import number_of_samples, unflatten_density

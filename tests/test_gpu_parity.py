@@ -11,7 +11,8 @@ pytestmark = pytest.mark.gpu
 CASES = ["qubit_couple_res_e2", "qubit_couple_res_e5", "qubit_couple_res_e3_e6",
          "qubit_t1_0K", "qubit_t1_mK", "qutrit_couple", "qutrit_couple_unital",
          "qubit_hyperfine", "qubit_couple_rot_e5", "spin1_c1", "nv7_n49",
-         "nv7_n19", "qubit_couple_nh", "qubit_couple_rot_nh"]
+         "nv7_n19", "qubit_couple_nh", "qubit_couple_rot_nh", "qubit_t1_0K_rot",
+         "qubit_t1_mK_rot_e2"]
 NONRES = ["qubit_couple", "qubit_couple_rot_e1_nores"]
 
 
