@@ -29,6 +29,8 @@ window.  Where the case is one of the reference's golden regression tests,
 the leading values of its CSV (``test/reference/*.csv``) are stored too.
 
 Run:  python tests/golden/make_golden.py            (about 5 minutes, 1 core)
+      python tests/golden/make_golden.py modes      (unitary / kernel mode arrays)
+      python tests/golden/make_golden.py csv        (the golden CSVs in full)
 """
 import math
 import os
@@ -459,6 +461,21 @@ def save_case(c, extra_runs=()):
           f"{_time.time() - t_start:.1f} s", flush=True)
 
 
+def save_reference_csvs():
+    """The reference's golden regression vectors in full
+    (``test/reference/*.csv``: every 29th value of the flattened
+    (T, n, n, re/im) density of a 10 us run at 1 ns, F = 100), as
+    ``reference_csv.npz``, keyed by CSV name."""
+    names = ["qubit-couple", "qubit-hyperfine", "qubit-t1-0K", "qubit-t1-mK",
+             "qutrit-couple", "qutrit-couple-unital", "qutrit-hyperfine"]
+    arrays = {}
+    for name in names:
+        path = os.path.join(REFERENCE, "test", "reference", name + ".csv")
+        arrays[name] = np.loadtxt(path, delimiter=",")
+    np.savez_compressed(os.path.join(HERE, "reference_csv.npz"), **arrays)
+    print("reference_csv:", {k: v.shape[0] for k, v in arrays.items()}, flush=True)
+
+
 def save_modes():
     """Operator (unitary) generators, elimination/duplication matrices and
     the equivalence-class projection of the reference for the qubit, qutrit
@@ -501,6 +518,9 @@ def main():
     only = set(sys.argv[1:])
     if "modes" in only:
         save_modes()
+        return
+    if "csv" in only:
+        save_reference_csvs()
         return
     save_quadratures()
     for c in cases():
