@@ -185,6 +185,21 @@ int sss_batch_run_table(sss_plan* plan, int ntraj, const double* rho0,
 int sss_batch_prepare(sss_plan* plan, int ntraj, const double* rho0, int nch,
                       int nseg, const double* programs, double dt, int F,
                       const double* readout_weights, void* cuda_stream);
+/* sss_batch_prepare for trajectories of uneven length: `samples` (host,
+ * ntraj) holds each trajectory's output-sample count, and every
+ * sss_batch_launch of the prepared batch must pass the same counts (as a
+ * device array).  Trajectories are then handed out longest first and,
+ * with automatic lanes (variant 0 or 4), the batch is also laid out for
+ * the wider lane groups that the trajectories still running call for as
+ * the shorter ones finish: a launch switches layout at the output samples
+ * where the running count stops filling the GPU, and cuts its grid to the
+ * trajectories still running, without allocating or synchronising (the
+ * chunks stay graph-capturable).  sss_batch_run does this by itself when
+ * it is given samples. */
+int sss_batch_prepare_samples(sss_plan* plan, int ntraj, const double* rho0,
+                              int nch, int nseg, const double* programs,
+                              const int* samples, double dt, int F,
+                              const double* readout_weights, void* cuda_stream);
 int sss_batch_launch(sss_plan* plan, double* state, const double* programs,
                      const int* samples, double t0, int t_begin, int n_samples,
                      int T_max, double* readout, void* cuda_stream);

@@ -26,7 +26,7 @@ SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
            "sss_plan_set_projection", "sss_plan_set_unitary",
            "sss_fp64_peak", "sss_fp64_mma_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
-           "sss_batch_launch", "sss_last_error",
+           "sss_batch_prepare_samples", "sss_batch_launch", "sss_last_error",
            "sss_plan_destroy"]
 
 
@@ -90,6 +90,8 @@ def load(build_if_missing=True):
         L.sss_adjoint_run.restype = i
         L.sss_batch_prepare.argtypes = [vp, i, vp, i, i, vp, d, i, dp, vp]
         L.sss_batch_prepare.restype = i
+        L.sss_batch_prepare_samples.argtypes = [vp, i, vp, i, i, vp, vp, d, i, dp, vp]
+        L.sss_batch_prepare_samples.restype = i
         L.sss_batch_launch.argtypes = [vp, vp, vp, vp, d, i, i, i, vp, vp]
         L.sss_batch_launch.restype = i
         L.sss_fp64_peak.restype = i
@@ -289,12 +291,21 @@ class Plan:
         return J, grad
 
     def batch_prepare(self, rho0_ptr, B, programs_ptr, nch, nseg, dt, F,
-                      readout_weights=None, stream=None):
-        """Analyse a batch (device pointers) and upload the kernel tables."""
+                      readout_weights=None, stream=None, samples=None):
+        """Analyse a batch (device pointers) and upload the kernel tables.
+        `samples` (host, B) -- the trajectories' output-sample counts, the
+        same as every launch passes -- prepares the phases of an uneven
+        batch (sss_batch_prepare_samples)."""
         rw = None if readout_weights is None else np.ascontiguousarray(
             readout_weights, dtype=np.float64)
-        check(load().sss_batch_prepare(self._h, B, rho0_ptr, nch, nseg, programs_ptr,
-                                       float(dt), int(F), dptr(rw), stream))
+        if samples is None:
+            check(load().sss_batch_prepare(self._h, B, rho0_ptr, nch, nseg, programs_ptr,
+                                           float(dt), int(F), dptr(rw), stream))
+        else:
+            smp = np.ascontiguousarray(samples, dtype=np.int32)
+            check(load().sss_batch_prepare_samples(self._h, B, rho0_ptr, nch, nseg, programs_ptr,
+                                                   smp.ctypes.data_as(ctypes.c_void_p), float(dt),
+                                                   int(F), dptr(rw), stream))
 
     def batch_launch(self, state_ptr, programs_ptr, t0, t_begin, n_samples, T_max,
                      samples_ptr=None, readout_ptr=None, stream=None):

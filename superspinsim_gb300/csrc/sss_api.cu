@@ -446,6 +446,22 @@ int sss_batch_prepare(sss_plan* p, int ntraj, const double* rho0, int nch, int n
                          (cudaStream_t)stream);
 }
 
+int sss_batch_prepare_samples(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                              const double* programs, const int* samples, double dt, int F,
+                              const double* readout_weights, void* stream) {
+    if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, 1, F, rho0)) return rc;
+    if (!programs) return fail(SSS_EINVAL, "batched runs need a coefficient program");
+    if (!samples) return fail(SSS_EINVAL, "null samples");
+    if (p->rotating && p->D + p->S == 0) return fail(SSS_EINVAL, "rotating tables not set");
+    if (p->n_full || p->u_n)
+        return fail(SSS_EINVAL, "batched runs support neither projected nor unitary plans");
+    if (ntraj == 0) return fail(SSS_EINVAL, "empty batch");
+    for (int b = 0; b < ntraj; b++)
+        if (samples[b] < 0) return fail(SSS_EINVAL, "samples[b] must not be negative");
+    return batch_prepare(p, ntraj, rho0, nch, nseg, programs, dt, F, readout_weights,
+                         (cudaStream_t)stream, nullptr, 0, samples);
+}
+
 int sss_batch_launch(sss_plan* p, double* state, const double* programs, const int* samples,
                      double t0, int t_begin, int n_samples, int T_max, double* readout,
                      void* stream) {
@@ -594,12 +610,13 @@ int sss_plan_batch_info(const sss_plan* p, int* lanes, int* degree, int* substep
 void sss_plan_destroy(sss_plan* p) {
     if (!p) return;
     DevBuf* bufs[] = {&p->d_gens, &p->d_dlast, &p->d_slast, &p->d_V, &p->d_Vinv,
-                      &p->d_sp_rowptr, &p->d_sp_col, &p->d_sp_val, &p->d_row_map,
+                      &p->d_sp_rowptr, &p->d_sp_col, &p->d_row_map,
                       &p->w_prop, &p->w_in, &p->w_out, &p->w_prog, &p->w_tab, &p->w_aux,
                       &p->w_queue, &p->w_ro, &p->w_fin, &p->w_samples, &p->w_status,
                       &p->w_state, &p->w_adjf, &p->w_adjb, &p->w_states, &p->w_adjro,
                       &p->w_adjst, &p->w_order};
     for (DevBuf* b : bufs) b->release();
+    for (DevBuf& b : p->batch_tables) b.release();
     if (p->ev_begin) cudaEventDestroy(p->ev_begin);
     if (p->ev_end) cudaEventDestroy(p->ev_end);
     delete p;

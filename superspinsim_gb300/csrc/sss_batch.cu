@@ -1653,71 +1653,119 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
     return SSS_OK;
 }
 
+// trajectories of a prepared batch with more than t output samples
+static int running_after(const sss_plan* p, int t) {
+    const std::vector<int>& lo = p->batch_longest;
+    return (int)(std::lower_bound(lo.begin(), lo.end(), t, std::greater<int>()) - lo.begin());
+}
+
 int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                   const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st,
-                  const double* d_tab, int T_tab) {
+                  const double* d_tab, int T_tab, const int* h_samples) {
     p->batch_ready = false;
     p->batch_empty = false;
+    p->batch_nphases = 0;
+    p->batch_longest.clear();
+    p->batch_order = nullptr;
     if (d_tab) {
         nch = p->d.G;
         nseg = 0;
     }
     p->batch_table = d_tab != nullptr;
-    BatchLayout Ly;
-    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st, false,
-                              d_tab, T_tab))
-        return rc;
-    if (Ly.M == 0) {
-        p->batch_ready = true;
-        p->batch_empty = true;
-        p->batch_ntraj = ntraj;
-        p->batch_nch = nch;
-        p->batch_nseg = nseg;
-        p->batch_dt = dt;
-        p->batch_F = F;
-        return SSS_OK;
-    }
-    BatchArgs a{};
-    size_t smem = 0;
-    if (int rc = make_args(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {}, p->d_sp_val, &a, &smem, st))
-        return rc;
-    static_assert(sizeof(BatchArgs) <= sizeof(p->batch_args), "BatchArgs does not fit the plan");
-    memcpy(p->batch_args, &a, sizeof(BatchArgs));
-    p->batch_smem = smem;
-    const int M = Ly.M, Ga = Ly.Ga, L = Ly.L, E = Ly.E, epl = Ly.epl, degree = Ly.degree,
-              substeps = Ly.substeps, threads = Ly.threads;
-    const bool use_reg = Ly.use_reg;
-    const bool one_chain = p->batch_variant == 3;
-    const long nnz = Ly.nnz;
-    p->batch_use_reg = use_reg;
-    p->batch_one_chain = one_chain;
-    p->batch_parts = Ly.parts;
-    p->batch_C = Ly.C;
-    p->batch_P = Ly.P;
-    p->batch_L = L;
-    p->batch_epl = epl;
-    p->batch_threads_used = threads;
     p->batch_ntraj = ntraj;
     p->batch_nch = nch;
     p->batch_nseg = nseg;
     p->batch_dt = dt;
     p->batch_F = F;
     p->batch_has_rw = h_rw != nullptr;
-    p->last_batch_lanes = L;
-    p->last_degree = degree;
-    p->last_substeps = substeps;
-    p->last_rows = M;
-    p->last_nnz = (int)nnz;
-    p->last_epl = E;
-    p->last_active = Ga;
-    p->last_variant = Ly.parts ? 4 : use_reg ? (one_chain ? 3 : 1) : 2;
+    // uneven lengths: hand trajectories out longest first, so that the
+    // groups sharing a warp run for about as long, the queue balances the
+    // tail, and the trajectories still running are always the first ones
+    // in the queue (longest-processing-time order)
+    if (h_samples && ntraj > 1) {
+        std::vector<int> order(ntraj);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return h_samples[x] > h_samples[y]; });
+        bool identity = true;
+        for (int i = 0; i < ntraj && identity; i++) identity = order[i] == i;
+        if (!identity) {
+            if (int rc = p->w_order.ensure(sizeof(int) * (size_t)ntraj)) return rc;
+            SSS_CUDA(cudaMemcpyAsync(p->w_order.p, order.data(), sizeof(int) * (size_t)ntraj,
+                                     cudaMemcpyHostToDevice, st));
+            SSS_CUDA(cudaStreamSynchronize(st));  // the host order goes out of scope
+            p->batch_order = p->w_order.as<int>();
+        }
+    }
+    // Phases.  The automatic lane count is the narrowest group that still
+    // gives every SM sub-partition a warp (n * L >= 4*32*SMs lanes).  With
+    // uneven lengths fewer groups remain as trajectories finish, whole
+    // sub-partitions idle and the longest trajectories run at the speed of
+    // one narrow group; so the batch is also laid out for the lane counts
+    // the trajectories still running call for, each from the output sample
+    // where the previous count stops meeting the rule (wider groups,
+    // shorter chains per trajectory).  A launch switches layout at those
+    // samples, as a chunked run switches chunks.
+    const bool phased = h_samples && ntraj > 1 && p->batch_lanes == 0 &&
+                        (p->batch_variant == 0 || p->batch_variant == 4);
+    if (phased) {
+        p->batch_longest.assign(h_samples, h_samples + ntraj);
+        std::sort(p->batch_longest.begin(), p->batch_longest.end(), std::greater<int>());
+    }
+    int t = 0;
+    for (int k = 0; k < kMaxPhases; k++) {
+        BatchLayout Ly;
+        p->auto_lanes_ntraj = phased ? std::max(1, running_after(p, t)) : 0;
+        int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {}, true, &Ly, st, false,
+                              d_tab, T_tab);
+        p->auto_lanes_ntraj = 0;
+        if (rc) return rc;
+        if (Ly.M == 0) {  // nothing reachable: the states stay as they are
+            p->batch_empty = true;
+            break;
+        }
+        if (k > 0 && Ly.L <= p->batch_phase[k - 1].L) break;  // no wider layout: phase k-1 runs on
+        BatchArgs a{};
+        size_t smem = 0;
+        if (int rc2 = make_args(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {}, p->batch_tables[k], &a,
+                                &smem, st))
+            return rc2;
+        sss_plan::BatchPhase& ph = p->batch_phase[k];
+        static_assert(sizeof(BatchArgs) <= sizeof(ph.args), "BatchArgs does not fit the plan");
+        memcpy(ph.args, &a, sizeof(BatchArgs));
+        ph.smem = smem;
+        ph.L = Ly.L;
+        ph.C = Ly.C;
+        ph.P = Ly.P;
+        ph.epl = Ly.epl;
+        ph.threads = Ly.threads;
+        ph.t_start = t;
+        ph.use_reg = Ly.use_reg;
+        ph.one_chain = p->batch_variant == 3;
+        ph.parts = Ly.parts;
+        p->batch_nphases = k + 1;
+        if (k == 0) {
+            p->last_batch_lanes = Ly.L;
+            p->last_degree = Ly.degree;
+            p->last_substeps = Ly.substeps;
+            p->last_rows = Ly.M;
+            p->last_nnz = (int)Ly.nnz;
+            p->last_epl = Ly.E;
+            p->last_active = Ly.Ga;
+            p->last_variant = Ly.parts ? 4 : Ly.use_reg ? (ph.one_chain ? 3 : 1) : 2;
+        }
+        if (!phased || !Ly.parts) break;
+        const long thr = (4L * 32 * p->num_sms + Ly.L - 1) / Ly.L;
+        if (thr > ntraj || p->batch_longest[thr - 1] <= t) break;
+        t = p->batch_longest[thr - 1];
+    }
     p->batch_ready = true;
     return SSS_OK;
 }
 
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st, double* d_trace, const int* d_order, const double* d_tab) {
+                 cudaStream_t st, double* d_trace, const double* d_tab) {
     if (!p->batch_ready) return fail(SSS_EINVAL, "no prepared batch (call sss_batch_prepare)");
     if (p->batch_table != (d_tab != nullptr))
         return fail(SSS_EINVAL, p->batch_table ? "the prepared batch runs from a coefficient table"
@@ -1729,55 +1777,81 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
                                        sizeof(double) * n_samples, p->batch_ntraj, st));
         return SSS_OK;
     }
-    BatchArgs a;
-    memcpy(&a, p->batch_args, sizeof(BatchArgs));
-    a.rho0 = d_state;
-    a.fin = d_state;
-    a.prog = d_prog;
-    a.samples = d_samples;
-    a.readout = d_readout;
-    a.trace = d_trace;
-    a.order = d_order;
-    a.tab = d_tab;
-    a.rw = d_readout ? a.rw : nullptr;
-    a.t0 = t0;
-    a.t_begin = t_begin;
-    a.t_end = t_begin + n_samples;
-    a.T_max = T_max;
-    SSS_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int), st));
-    const int L = p->batch_L, epl = p->batch_epl, threads = p->batch_threads_used;
-    const bool use_reg = p->batch_use_reg, one_chain = p->batch_one_chain;
-    const size_t smem = p->batch_smem;
-    int rc;
-    if (p->batch_parts) {
-        switch (L) {
-            case 8: rc = launch_parts<8>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
-            case 16: rc = launch_parts<16>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
-            case 32: rc = launch_parts<32>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
-            case 64: rc = launch_parts<64>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
-            case 128: rc = launch_parts<128>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
-            default: rc = launch_parts<256>(p, p->batch_C, p->batch_P, a, threads, smem, st); break;
+    // The samples [t_begin, t_end) run as one launch per phase they touch,
+    // and a phase's launch is cut again where the number of trajectories
+    // still running halves (while at least two per SM remain): every launch
+    // has one group per running trajectory, which the queue hands the
+    // running ones first, so its CTAs spread evenly over the SMs.
+    const int t_end = t_begin + n_samples;
+    int launches = 0, rc = SSS_OK;
+    for (int t = t_begin; t < t_end && rc == SSS_OK;) {
+        int k = 0;
+        while (k + 1 < p->batch_nphases && p->batch_phase[k + 1].t_start <= t) k++;
+        int stop = t_end;
+        if (k + 1 < p->batch_nphases) stop = std::min(stop, p->batch_phase[k + 1].t_start);
+        int n_running = 0;
+        if (!p->batch_longest.empty()) {
+            n_running = running_after(p, t);
+            if (n_running >= 4 * p->num_sms) {
+                const int half_at = p->batch_longest[n_running / 2 - 1];
+                if (half_at > t) stop = std::min(stop, half_at);
+            }
         }
-    } else if (use_reg) {
-        switch (L) {
-            case 1: rc = launch_reg<1>(p, epl, a, threads, smem, st, one_chain); break;
-            case 2: rc = launch_reg<2>(p, epl, a, threads, smem, st, one_chain); break;
-            case 4: rc = launch_reg<4>(p, epl, a, threads, smem, st, one_chain); break;
-            case 8: rc = launch_reg<8>(p, epl, a, threads, smem, st, one_chain); break;
-            case 16: rc = launch_reg<16>(p, epl, a, threads, smem, st, one_chain); break;
-            default: rc = launch_reg<32>(p, epl, a, threads, smem, st, one_chain); break;
+        const sss_plan::BatchPhase& ph = p->batch_phase[k];
+        BatchArgs a;
+        memcpy(&a, ph.args, sizeof(BatchArgs));
+        a.rho0 = d_state;
+        a.fin = d_state;
+        a.prog = d_prog;
+        a.samples = d_samples;
+        a.readout = d_readout;
+        a.trace = d_trace;
+        a.order = p->batch_order;
+        a.tab = d_tab;
+        a.rw = d_readout ? a.rw : nullptr;
+        a.t0 = t0;
+        a.t_begin = t;
+        a.t_end = stop;
+        a.T_max = T_max;
+        SSS_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int), st));
+        const int L = ph.L, epl = ph.epl, threads = ph.threads;
+        const size_t smem = ph.smem;
+        p->ev_keep_begin = launches > 0;
+        p->launch_active = n_running;
+        if (ph.parts) {
+            switch (L) {
+                case 8: rc = launch_parts<8>(p, ph.C, ph.P, a, threads, smem, st); break;
+                case 16: rc = launch_parts<16>(p, ph.C, ph.P, a, threads, smem, st); break;
+                case 32: rc = launch_parts<32>(p, ph.C, ph.P, a, threads, smem, st); break;
+                case 64: rc = launch_parts<64>(p, ph.C, ph.P, a, threads, smem, st); break;
+                case 128: rc = launch_parts<128>(p, ph.C, ph.P, a, threads, smem, st); break;
+                default: rc = launch_parts<256>(p, ph.C, ph.P, a, threads, smem, st); break;
+            }
+        } else if (ph.use_reg) {
+            switch (L) {
+                case 1: rc = launch_reg<1>(p, epl, a, threads, smem, st, ph.one_chain); break;
+                case 2: rc = launch_reg<2>(p, epl, a, threads, smem, st, ph.one_chain); break;
+                case 4: rc = launch_reg<4>(p, epl, a, threads, smem, st, ph.one_chain); break;
+                case 8: rc = launch_reg<8>(p, epl, a, threads, smem, st, ph.one_chain); break;
+                case 16: rc = launch_reg<16>(p, epl, a, threads, smem, st, ph.one_chain); break;
+                default: rc = launch_reg<32>(p, epl, a, threads, smem, st, ph.one_chain); break;
+            }
+        } else {
+            switch (L) {
+                case 1: rc = launch(p, k_batch_lanes<1>, a, threads, threads, smem, st); break;
+                case 2: rc = launch(p, k_batch_lanes<2>, a, threads, threads / 2, smem, st); break;
+                case 4: rc = launch(p, k_batch_lanes<4>, a, threads, threads / 4, smem, st); break;
+                case 8: rc = launch(p, k_batch_lanes<8>, a, threads, threads / 8, smem, st); break;
+                case 16: rc = launch(p, k_batch_lanes<16>, a, threads, threads / 16, smem, st); break;
+                default: rc = launch(p, k_batch_lanes<32>, a, threads, threads / 32, smem, st); break;
+            }
         }
-    } else {
-        switch (L) {
-            case 1: rc = launch(p, k_batch_lanes<1>, a, threads, threads, smem, st); break;
-            case 2: rc = launch(p, k_batch_lanes<2>, a, threads, threads / 2, smem, st); break;
-            case 4: rc = launch(p, k_batch_lanes<4>, a, threads, threads / 4, smem, st); break;
-            case 8: rc = launch(p, k_batch_lanes<8>, a, threads, threads / 8, smem, st); break;
-            case 16: rc = launch(p, k_batch_lanes<16>, a, threads, threads / 16, smem, st); break;
-            default: rc = launch(p, k_batch_lanes<32>, a, threads, threads / 32, smem, st); break;
-        }
+        p->ev_keep_begin = false;
+        p->launch_active = 0;
+        if (rc == SSS_OK) launches++;
+        t = stop;
     }
-    p->last_launches = rc == SSS_OK ? 1 : 0;
+    p->last_launches = launches;
     return rc;
 }
 
@@ -1834,27 +1908,11 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
               const double* h_rw, double* d_readout, double* d_final, cudaStream_t st,
               double* d_trace, const double* d_tab) {
     const int N = p->d.N;
-    // uneven lengths: hand trajectories out longest first, so that the
-    // groups sharing a warp run for about as long and the queue balances
-    // the tail (longest-processing-time order)
-    const int* d_order = nullptr;
-    if (h_samples && ntraj > 1) {
-        std::vector<int> order(ntraj);
-        std::iota(order.begin(), order.end(), 0);
-        std::stable_sort(order.begin(), order.end(),
-                         [&](int x, int y) { return h_samples[x] > h_samples[y]; });
-        bool identity = true;
-        for (int i = 0; i < ntraj && identity; i++) identity = order[i] == i;
-        if (!identity) {
-            if (int rc = p->w_order.ensure(sizeof(int) * (size_t)ntraj)) return rc;
-            SSS_CUDA(cudaMemcpyAsync(p->w_order.p, order.data(), sizeof(int) * (size_t)ntraj,
-                                     cudaMemcpyHostToDevice, st));
-            SSS_CUDA(cudaStreamSynchronize(st));  // the host order goes out of scope
-            d_order = p->w_order.as<int>();
-        }
-    }
     if (d_trace)
         SSS_CUDA(cudaMemsetAsync(d_trace, 0, sizeof(double) * (size_t)ntraj * T_max * N, st));
+    if (int rc = batch_prepare(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, h_rw, st, d_tab, T_max,
+                               h_samples))
+        return rc;
     // the launches run in place on a state buffer that starts as rho0
     double* state = d_final;
     if (!state) {
@@ -1864,57 +1922,8 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, c
     if (state != d_rho0)
         SSS_CUDA(cudaMemcpyAsync(state, d_rho0, sizeof(double) * (size_t)ntraj * N,
                                  cudaMemcpyDeviceToDevice, st));
-    // Uneven lengths with automatic lanes run in phases.  The automatic lane
-    // count is the narrowest group that still gives every SM sub-partition a
-    // warp; as trajectories finish, fewer groups remain, whole sub-partitions
-    // idle and the longest trajectories run at the speed of one narrow group.
-    // So the run stops where the trajectories still running no longer meet
-    // the lane rule and the rest is prepared again (from the current states)
-    // with the lane count the remaining trajectories call for: wider groups,
-    // shorter chains per trajectory.  Finished trajectories stay in the queue
-    // (they only pad their readout rows).  A phase ends on an output sample,
-    // as a chunked run does.
-    std::vector<int> longest;  // sample counts, longest first
-    const bool phased = h_samples && ntraj > 1 && p->batch_lanes == 0 &&
-                        (p->batch_variant == 0 || p->batch_variant == 4);
-    if (phased) {
-        longest.assign(h_samples, h_samples + ntraj);
-        std::sort(longest.begin(), longest.end(), std::greater<int>());
-    }
-    const double* prep_src = d_rho0;
-    int t = 0, launches = 0, prev_L = 0;
-    int rc = SSS_OK;
-    while (rc == SSS_OK && t < T_max) {
-        // trajectories with more than t samples: the lane rule's count and
-        // the groups the launch needs (0: the whole batch)
-        const int n_running =
-            phased ? std::max<int>(1, (int)(std::lower_bound(longest.begin(), longest.end(), t,
-                                                             std::greater<int>()) -
-                                            longest.begin()))
-                   : 0;
-        p->auto_lanes_ntraj = n_running;
-        rc = batch_prepare(p, ntraj, prep_src, nch, nseg, d_prog, dt, F, h_rw, st, d_tab, T_max);
-        p->auto_lanes_ntraj = 0;
-        if (rc) break;
-        int t_end = T_max;
-        if (phased && p->batch_parts && !p->batch_empty && p->batch_L > prev_L && launches < 8) {
-            // the lane rule holds while n * L >= 4*32*SMs trajectories' lanes
-            const long thr = (4L * 32 * p->num_sms + p->batch_L - 1) / p->batch_L;
-            if (thr <= ntraj && longest[thr - 1] > t) t_end = std::min(T_max, longest[thr - 1]);
-        }
-        prev_L = p->batch_L;
-        p->ev_keep_begin = launches > 0;
-        p->launch_active = n_running;
-        rc = batch_launch(p, state, d_prog, d_samples, t0, t, t_end - t, T_max, d_readout, st,
-                          d_trace, d_order, d_tab);
-        p->ev_keep_begin = false;
-        p->launch_active = 0;
-        launches += p->last_launches;
-        prep_src = state;
-        t = t_end;
-    }
-    p->last_launches = launches;
-    return rc;
+    return batch_launch(p, state, d_prog, d_samples, t0, 0, T_max, T_max, d_readout, st, d_trace,
+                        d_tab);
 }
 
 }  // namespace sss

@@ -14,7 +14,8 @@ constexpr int kMaxG = 8;      // generators per frame
 constexpr int kMaxQ = 3;      // Gauss-Legendre nodes
 constexpr int kMaxK = 6;      // exponentials per step
 constexpr int kMaxCh = 4;     // coefficient channels
-constexpr int kMaxSlots = kMaxQ * kMaxG;  // generator slots of a rotating plan (node, generator)
+constexpr int kMaxSlots = kMaxQ * kMaxG;
+constexpr int kMaxPhases = 6;  // lane counts of a prepared batch (8 .. 256)  // generator slots of a rotating plan (node, generator)
 constexpr int kPlainMaxN = 52;  // dense shared-memory propagator path
 // row-part kernels (forward and adjoint)
 constexpr int kCloseMax = 8;    // close slots per lane
@@ -90,7 +91,7 @@ struct sss_plan {
     sss::SparseGenerators sparse;    // lab frame, for sss_batch_run
     // device copies
     sss::DevBuf d_gens, d_dlast, d_slast, d_V, d_Vinv;
-    sss::DevBuf d_sp_rowptr, d_sp_col, d_sp_val;
+    sss::DevBuf d_sp_rowptr, d_sp_col;
     sss::DevBuf d_row_map;
     // workspace
     sss::DevBuf w_prop, w_in, w_out, w_prog, w_tab, w_aux, w_queue, w_ro,
@@ -109,16 +110,24 @@ struct sss_plan {
     bool ev_keep_begin = false;  // a later phase of one run: keep the first launch's begin event
     int auto_lanes_ntraj = 0;    // trajectories the automatic lane rule counts (0: the batch)
     int launch_active = 0;       // trajectories with work in the next launch (0: the batch)
-    // prepared batch (sss_batch_prepare -> sss_batch_launch)
-    alignas(16) unsigned char batch_args[1024];
-    bool batch_ready = false, batch_empty = false, batch_use_reg = false,
-         batch_one_chain = false, batch_has_rw = false, batch_parts = false,
-         batch_table = false;
-    int batch_C = 0, batch_P = 0;
-    int batch_L = 0, batch_epl = 0, batch_threads_used = 0, batch_ntraj = 0, batch_nch = 0,
-        batch_nseg = 0, batch_F = 0;
+    // prepared batch (sss_batch_prepare -> sss_batch_launch): one kernel
+    // layout per phase -- a single phase, or with uneven lengths and
+    // automatic lanes one per widening lane count, phase k running from
+    // output sample t_start on
+    struct BatchPhase {
+        alignas(16) unsigned char args[1024];
+        size_t smem = 0;
+        int L = 0, C = 0, P = 0, epl = 0, threads = 0, t_start = 0;
+        bool use_reg = false, one_chain = false, parts = false;
+    };
+    BatchPhase batch_phase[sss::kMaxPhases];
+    sss::DevBuf batch_tables[sss::kMaxPhases];
+    int batch_nphases = 0;
+    std::vector<int> batch_longest;    // the prepared sample counts, longest first (or empty)
+    const int* batch_order = nullptr;  // queue position -> trajectory, longest first (w_order)
+    bool batch_ready = false, batch_empty = false, batch_has_rw = false, batch_table = false;
+    int batch_ntraj = 0, batch_nch = 0, batch_nseg = 0, batch_F = 0;
     double batch_dt = 0.0;
-    size_t batch_smem = 0;
     sss::DevBuf w_state;
     // adjoint (row-part path): forward and backward tables, stored states,
     // readouts, state buffer
@@ -155,13 +164,15 @@ int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 const double* h_tw, double* d_J, double* d_grad, cudaStream_t st);
 // d_tab: a coefficient table (ntraj*(F*T_tab*Q)*G, rows (r*T_tab + t)*Q + k)
 // in place of the programs; it runs on the row-part kernel
+// h_samples: the trajectories' output-sample counts (host), or null; with
+// them trajectories are handed out longest first and, with automatic lanes,
+// the batch is prepared in phases
 int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                   const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st,
-                  const double* d_tab = nullptr, int T_tab = 0);
+                  const double* d_tab = nullptr, int T_tab = 0, const int* h_samples = nullptr);
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
-                 cudaStream_t st, double* d_trace = nullptr, const int* d_order = nullptr,
-                 const double* d_tab = nullptr);
+                 cudaStream_t st, double* d_trace = nullptr, const double* d_tab = nullptr);
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
                  bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts = false,

@@ -171,9 +171,11 @@ class ChunkedRun:
         self.t_next = 0
         self.graph = None
         stream = torch.cuda.current_stream().cuda_stream
+        # with uneven lengths the prepared batch also holds the layouts of
+        # its later phases (wider lane groups as trajectories finish)
         sweep.plan.batch_prepare(self.rho0.data_ptr(), self.B, self.programs.data_ptr(),
                                  progs.shape[1], progs.shape[2], self.dt, sweep.F,
-                                 readout_weights, stream=stream)
+                                 readout_weights, stream=stream, samples=samples)
 
     def _launch(self, t_begin, n):
         self.sweep.plan.batch_launch(

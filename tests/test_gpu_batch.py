@@ -265,3 +265,52 @@ def test_dropin_simulate_nv21_uses_batched_trace():
                              F=50, vectorisation_map=vm, mode="vector", degree=16)
     assert d.shape == (3, 21, 21)
     assert np.abs(d - ref).max() <= 1e-12
+
+
+def test_phased_uneven_batch_chunked_graph_and_oracle():
+    """3000 short uneven Ramsey trajectories: enough for the automatic lanes
+    to widen in phases (8 lanes while 2432 or more run, then 16, then 32).
+    The one-shot run, a chunked run and its CUDA-graph capture -- all
+    prepared with the sample counts -- agree bit for bit (the same layout
+    at every output sample), and sampled trajectories match the oracle."""
+    torch = pytest.importorskip("torch")
+    from superspinsim_gb300 import protocols
+    from superspinsim_gb300.sweep import ChunkedRun, Sweep, population_weights
+    c = load_case("nv7_n49")
+    gens, vm = c["generators"], c["vectorisation_map"]
+    f_res = 2.870e9 + 28.025e9*5e-3
+    rng = np.random.default_rng(11)
+    B = 3000
+    progs, dur = protocols.ramsey(rng.uniform(40e6, 80e6, B), rng.uniform(-5e6, 5e6, B),
+                                  rng.uniform(0, 30e-9, B), f_res, 10/65.9, t_init=4e-9,
+                                  t_read=3e-9)
+    dt, F = 1e-9, 10
+    samples = np.ceil(dur/dt).astype(np.int32)
+    T = int(samples.max())
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1
+    w = population_weights(vm, [3, 4, 5])
+    sw = Sweep(gens, vm, number_of_exponentials=2, number_of_fine_divisions=F)
+    one = sw.run(rho, progs, 0.0, T*dt + 1e-13, dt, samples=samples, readout_weights=w,
+                 final_state=True)
+    assert sw.plan.last_launches() >= 3     # three lane counts, at least
+    run = ChunkedRun(sw, rho, progs, 0.0, dt, T, samples=samples, readout_weights=w).run(chunk=7)
+    r = run.results()
+    assert np.array_equal(r["readout"], one["readout"])
+    assert np.array_equal(r["final"], one["final"])
+    g = ChunkedRun(sw, rho, progs, 0.0, dt, T, samples=samples, readout_weights=w)
+    g.capture(chunk=9).replay()
+    torch.cuda.synchronize()
+    r2 = g.results()
+    assert np.array_equal(r2["readout"], one["readout"])
+    assert np.array_equal(r2["final"], one["final"])
+    W, nodes = quadrature(2)
+    order = np.argsort(samples)
+    for b in (order[0], order[B//2], order[-1], 17):
+        n = int(samples[b])
+        _, ref = oracle.simulate(gens, rho, 0.0, n*dt + 1e-13, dt, progs[b], K=2, W=W,
+                                 nodes=nodes, F=F, vectorisation_map=vm, mode="vector",
+                                 degree=16, flat_out=True)
+        assert np.abs(one["final"][b] - ref[-1]).max() <= 1e-12
+        assert np.abs(one["readout"][b, :n] - ref @ w).max() <= 1e-12
+        assert np.all(one["readout"][b, n:] == 0.0)
