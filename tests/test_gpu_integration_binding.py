@@ -1,7 +1,8 @@
 """The reference-side binding of the integration notes: plain ctypes on
 libsss.so (no package helpers), as a maintainer of the reference would add
-it -- sss_simulate with a host-sampled coefficient table and sss_batch_run
-for a sweep -- against the oracle."""
+it -- sss_simulate with a host-sampled coefficient table, sss_batch_run for
+a sweep of programs and sss_batch_run_table for the same sweep from sampled
+rows -- against the oracle."""
 import ctypes
 
 import numpy as np
@@ -33,6 +34,10 @@ def _bind():
     lib.sss_batch_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_int,
                                   _dp, _ip, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int, ctypes.c_void_p]
+    lib.sss_batch_run_table.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                        ctypes.c_void_p]
     lib.sss_last_error.restype = ctypes.c_char_p
     lib.sss_plan_destroy.argtypes = [ctypes.c_void_p]
     return lib
@@ -96,5 +101,19 @@ def test_reference_side_ctypes_binding():
                                   degree=16, flat_out=True)
         assert np.abs(fin - refb[:, -1]).max() <= 1e-12
         assert np.abs(ro - refb @ w).max() <= 1e-12
+        # sss_batch_run_table: the same sweep from sampled rows (a sampler
+        # callable per trajectory), as the integration notes bind it
+        tabs = np.zeros((4, F*T*Q, G))
+        for b, f in enumerate(freqs):
+            for r in range(F):
+                for t in range(T):
+                    for k in range(Q):
+                        tn = ((0.0 + (r*dt)/F) + dt*t) + (dt*nodes[k])/F
+                        tabs[b, (r*T + t)*Q + k] = [1.0, amp*np.cos(2*np.pi*f*tn), 0, 0, laser]
+        ro2, fin2 = np.empty((4, T)), np.empty((4, N))
+        check(lib.sss_batch_run_table(plan, 4, _p(rho0), _p(tabs), None, 0.0, dt, T, F, _p(w),
+                                      _p(ro2), _p(fin2), None, 1, None))
+        assert np.abs(fin2 - refb[:, -1]).max() <= 1e-12
+        assert np.abs(ro2 - refb @ w).max() <= 1e-12
     finally:
         lib.sss_plan_destroy(plan)
