@@ -262,7 +262,10 @@ int sss_plan_last_launches(const sss_plan* plan);
  * 2 = always the shared-memory variant; 3 = register variant with one FMA
  * chain per row; 4 = row-part variant: rows cut into parts of a few
  * entries, each lane running C equal-length FMA chains, 8, 16 or 32 lanes,
- * small patterns only -- SSS_EINVAL when the pattern does not fit).  No
+ * small patterns only -- SSS_EINVAL when the pattern does not fit; 5 = as
+ * 4, with the state in registers moved by warp shuffles where the layout
+ * allows it: 32 lanes, one chain per lane, no lane owning two rows, lab
+ * frame).  No
  * reference counterpart (the reference's launch shapes are fixed,
  * generate_simulator.py:85-106). */
 int sss_plan_set_batch_config(sss_plan* plan, int lanes, int cta_threads,

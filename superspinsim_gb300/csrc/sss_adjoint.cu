@@ -928,10 +928,10 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
 int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 const double* d_prog, double t0, double dt, int T, int F, const double* h_rw,
                 const double* h_tw, double* d_J, double* d_grad, cudaStream_t st) {
-    if (p->batch_variant == 0 || p->batch_variant == 4) {
+    if (p->batch_variant == 0 || p->batch_variant == 4 || p->batch_variant == 5) {
         const int rc = adjoint_run_parts(p, ntraj, d_rho0, nch, nseg, d_prog, t0, dt, T, F, h_rw,
                                          h_tw, d_J, d_grad, st);
-        if (rc != SSS_EINVAL || p->batch_variant == 4) return rc;
+        if (rc != SSS_EINVAL || p->batch_variant == 4 || p->batch_variant == 5) return rc;
         set_error("");
     }
     const int N = p->d.N, K = p->d.K, Q = p->d.Q;

@@ -574,7 +574,7 @@ int sss_plan_set_batch_config(sss_plan* p, int lanes, int cta_threads, int varia
         return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part variant");
     if (cta_threads != 0 && (cta_threads < 32 || cta_threads > 256 || cta_threads % 32))
         return fail(SSS_EINVAL, "cta_threads must be 0 or a multiple of 32 in [32, 256]");
-    if (variant < 0 || variant > 4) return fail(SSS_EINVAL, "variant must be 0, 1, 2, 3 or 4");
+    if (variant < 0 || variant > 5) return fail(SSS_EINVAL, "variant must be 0, 1, 2, 3, 4 or 5");
     p->batch_lanes = lanes;
     p->batch_threads = cta_threads;
     p->batch_variant = variant;

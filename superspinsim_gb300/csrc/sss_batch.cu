@@ -813,6 +813,155 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
     }
 }
 
+// Register-state form of the row-part kernel, for one trajectory per warp
+// (32 lanes, one chain of P entries per lane) when no lane owns more than
+// one row (NV-7: 19 rows in 29 parts).  Each row's value lives in a
+// register of its owner lane and moves by warp shuffles: a part fetches its
+// columns from their owners, and an owner fetches its row's partial sums
+// from the part lanes (padding close slots fetch from a lane whose parts are
+// all padding, so they add zero).  There is no shared-memory state, no
+// barrier inside a Horner term and no bank conflict; the coefficient ring
+// is the row-part kernel's.  Lab frame, no stored states.
+template <int P>
+__global__ void __launch_bounds__(256, 1) k_batch_shfl(const BatchArgs a) {
+    extern __shared__ double smem[];
+    constexpr int L = 32;
+    constexpr unsigned kFull = 0xffffffffu;
+    const int M = a.M, NL = a.n_live, NC = a.n_lch, K = a.K, Q = a.Q;
+    const int Ms = M + 2;
+    const int slot = threadIdx.x / L, li = threadIdx.x % L;
+    // the row-part kernel's per-trajectory layout (only the ring is used)
+    const size_t per_slot = (3 * (size_t)Ms + L + 1 + (size_t)kRing * (Q * NC + K * NL)) | 1;
+    double* ringc = smem + slot * per_slot + 3 * (size_t)Ms + L + 1;
+    double* ring_ag = ringc + kRing * Q * NC;
+    double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
+    for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw ? a.rw[i] : 0.0;
+    const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
+    const int my_row = r1 > r0 ? r0 : -1;
+    // owner lane of each part column (the zero row: this lane, weight 0)
+    int src[P];
+    bool all_pad = true;
+#pragma unroll
+    for (int q = 0; q < P; q++) {
+        const int c = __ldg(a.pcol + (size_t)q * L + li);
+        int owner = li;
+        if (c < M) {
+            all_pad = false;
+            for (int l = 0; l < L; l++)
+                if (__ldg(a.rbeg + l) <= c && c < __ldg(a.rbeg + l + 1)) owner = l;
+        }
+        src[q] = owner;
+    }
+    const unsigned pad_lanes = __ballot_sync(kFull, all_pad);
+    const int zero_lane = pad_lanes ? __ffs(pad_lanes) - 1 : li;
+    int pl[kCloseMax];
+#pragma unroll
+    for (int k = 0; k < kCloseMax; k++) {
+        const int part = (int)((__ldg(a.cw + (size_t)k * L + li) >> 16) & 0x7fffu);
+        pl[k] = part < L ? part : zero_lane;
+    }
+    const int kc = a.kc;
+    __syncthreads();
+
+    int b = -1, T_b = 0, t = 0, r = 0, rp = kRing;
+    const double* prog = nullptr;
+    double om[P];
+    double v = 0.0;  // this lane's row of the state
+    while (true) {
+        if (r == 0 && t >= T_b) {
+            if (b >= 0 && a.fin && my_row >= 0) a.fin[(size_t)b * a.N + a.row_orig[my_row]] = v;
+            if (b >= 0 && a.readout)
+                for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
+                    a.readout[(size_t)b * a.T_max + tt] = 0.0;
+            int nb = 0;
+            if (li == 0) nb = atomicAdd(a.queue, 1);
+            nb = __shfl_sync(kFull, nb, 0);
+            b = nb;
+            if (b >= a.ntraj) break;
+            if (a.order) b = __ldg(a.order + b);
+            T_b = min(a.samples ? a.samples[b] : a.T_max, a.t_end);
+            t = a.t_begin;
+            rp = kRing;
+            prog = a.prog ? a.prog + (size_t)b * a.nch * a.nseg * 5 : nullptr;
+            v = my_row >= 0 ? a.rho0[(size_t)b * a.N + a.row_orig[my_row]] : 0.0;
+            __syncwarp(kFull);
+            if (t >= T_b) continue;
+        }
+        if (rp == kRing) {
+            for (int i = li; i < kRing * Q * NC; i += L) {
+                const int s = i / (Q * NC), rem = i - s * Q * NC, k = rem / NC, ci = rem - k * NC;
+                const int rr = r + s, ts = t + rr / a.F, rs = rr % a.F;
+                const int ch = a.lch_chan[ci];
+                double val = 0.0;
+                if (a.tab) {
+                    if (ts < a.T_max)
+                        val = __ldg(a.tab + (((size_t)b * a.F + rs) * a.T_max + ts) * (size_t)(Q * a.tab_G) +
+                                    (size_t)k * a.tab_G + ch);
+                } else if (ch < a.nch) {
+                    const double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + rs)),
+                                                          __dmul_rn(a.dt, (double)ts)),
+                                                __ldg(a.noff + k));
+                    val = channel_value(prog, a.nseg, ch, tn);
+                }
+                ringc[i] = val;
+            }
+            __syncwarp(kFull);
+            for (int i = li; i < kRing * K * NL; i += L) {
+                const int s = i / (K * NL), rem = i - s * K * NL, e = rem / NL, gi = rem - e * NL;
+                const int ci = a.live_ch[gi];
+                double w = 0.0;
+                for (int k = 0; k < Q; k++) w = fma(__ldg(a.W + e * Q + k), ringc[(s * Q + k) * NC + ci], w);
+                ring_ag[i] = w * a.h_sub;
+            }
+            __syncwarp(kFull);
+            rp = 0;
+        }
+        for (int e_exp = K - 1; e_exp >= 0; e_exp--) {
+            const double* o0 = a.om0 + (size_t)e_exp * P * L + li;
+#pragma unroll
+            for (int e = 0; e < P; e++) om[e] = __ldg(o0 + (size_t)e * L);
+            for (int gi = 0; gi < NL; gi++) {
+                const double c = ring_ag[(rp * K + e_exp) * NL + gi];
+                if (c == 0.0) continue;
+                const double* gv = a.gv + (size_t)a.live[gi] * P * L + li;
+#pragma unroll
+                for (int e = 0; e < P; e++) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);
+            }
+            for (int m = 0; m < a.substeps; m++) {
+                // Horner: w <- v + (Omega w)/j for j = d..1, starting at w = v
+                double cur = v;
+                for (int j = a.degree; j >= 1; j--) {
+                    const double ij = a.inv_j[j];
+                    double s = 0.0;
+#pragma unroll
+                    for (int q = 0; q < P; q++) s = fma(om[q], __shfl_sync(kFull, cur, src[q]), s);
+                    double acc = v;
+#pragma unroll
+                    for (int k = 0; k < kCloseMax; k++) {
+                        if (k >= kc) break;
+                        acc = fma(__shfl_sync(kFull, s, pl[k]), ij, acc);
+                    }
+                    cur = acc;
+                }
+                v = cur;
+            }
+        }
+        rp++;
+        if (++r == a.F) {
+            r = 0;
+            if (a.trace && my_row >= 0)
+                a.trace[((size_t)b * a.T_max + t) * a.N + a.row_orig[my_row]] = v;
+            if (a.readout) {
+                double s = my_row >= 0 ? s_rw[my_row] * v : 0.0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+            }
+            t++;
+        }
+    }
+}
+
 template <class Kern>
 int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_per_cta,
            size_t smem, cudaStream_t st) {
@@ -1328,11 +1477,12 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
     // Automatic lanes: 32 (one trajectory per warp, the shortest chains)
     // while the batch gives at most two warps per SM sub-partition, else 16
     // (two trajectories per warp, fewer instructions per trajectory)
-    if (rot && !force_parts && allow_register && p->batch_variant != 0 && p->batch_variant != 4)
+    const bool parts_asked = p->batch_variant == 4 || p->batch_variant == 5;
+    if (rot && !force_parts && allow_register && p->batch_variant != 0 && !parts_asked)
         return fail(SSS_EINVAL, "the rotating frame runs on the row-part kernel (variant 0 or 4)");
-    if (table && !force_parts && p->batch_variant != 0 && p->batch_variant != 4)
+    if (table && !force_parts && p->batch_variant != 0 && !parts_asked)
         return fail(SSS_EINVAL, "a coefficient table runs on the row-part kernel (variant 0 or 4)");
-    if (force_parts || (allow_register && (rot || table || p->batch_variant == 4 ||
+    if (force_parts || (allow_register && (rot || table || parts_asked ||
                                            p->batch_variant == 0))) {
         // lanes: as configured, or the narrowest group (fewest instructions
         // per trajectory) that still gives every SM sub-partition a warp and
@@ -1368,7 +1518,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
             Ly.degree = degree;
             Ly.substeps = substeps;
         }
-        if (rc == SSS_OK || p->batch_variant == 4 || force_parts || rot || table) return rc;
+        if (rc == SSS_OK || parts_asked || force_parts || rot || table) return rc;
     }
     if (L > 32)
         return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part variant, "
@@ -1707,7 +1857,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     // shorter chains per trajectory).  A launch switches layout at those
     // samples, as a chunked run switches chunks.
     const bool phased = h_samples && ntraj > 1 && p->batch_lanes == 0 &&
-                        (p->batch_variant == 0 || p->batch_variant == 4);
+                        (p->batch_variant == 0 || p->batch_variant == 4 || p->batch_variant == 5);
     if (phased) {
         p->batch_longest.assign(h_samples, h_samples + ntraj);
         std::sort(p->batch_longest.begin(), p->batch_longest.end(), std::greater<int>());
@@ -1743,6 +1893,20 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
         ph.use_reg = Ly.use_reg;
         ph.one_chain = p->batch_variant == 3;
         ph.parts = Ly.parts;
+        // the register-state form: one trajectory per warp, one chain per
+        // lane, no lane owning two rows, and a lane whose parts are all
+        // padding (the zero partial of the padding close slots); lab frame
+        ph.shfl = false;
+        if (p->batch_variant == 5 && Ly.parts && Ly.L == 32 && Ly.C == 1 && !p->rotating) {
+            bool ok = true, pad_lane = false;
+            for (int l = 0; l < Ly.L && ok; l++) ok = Ly.lane_of[l].size() <= 1;
+            for (int l = 0; l < Ly.L && !pad_lane; l++) {
+                bool all = true;
+                for (int q = 0; q < Ly.P; q++) all = all && Ly.pcol[(size_t)q * Ly.L + l] == Ly.M;
+                pad_lane = all;
+            }
+            ph.shfl = ok && pad_lane && (Ly.P == 4 || Ly.P == 8);
+        }
         p->batch_nphases = k + 1;
         if (k == 0) {
             p->last_batch_lanes = Ly.L;
@@ -1818,7 +1982,10 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
         const size_t smem = ph.smem;
         p->ev_keep_begin = launches > 0;
         p->launch_active = n_running;
-        if (ph.parts) {
+        if (ph.shfl) {
+            rc = ph.P == 4 ? launch(p, k_batch_shfl<4>, a, threads, threads / 32, smem, st)
+                           : launch(p, k_batch_shfl<8>, a, threads, threads / 32, smem, st);
+        } else if (ph.parts) {
             switch (L) {
                 case 8: rc = launch_parts<8>(p, ph.C, ph.P, a, threads, smem, st); break;
                 case 16: rc = launch_parts<16>(p, ph.C, ph.P, a, threads, smem, st); break;

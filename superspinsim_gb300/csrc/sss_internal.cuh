@@ -118,7 +118,7 @@ struct sss_plan {
         alignas(16) unsigned char args[1024];
         size_t smem = 0;
         int L = 0, C = 0, P = 0, epl = 0, threads = 0, t_start = 0;
-        bool use_reg = false, one_chain = false, parts = false;
+        bool use_reg = false, one_chain = false, parts = false, shfl = false;
     };
     BatchPhase batch_phase[sss::kMaxPhases];
     sss::DevBuf batch_tables[sss::kMaxPhases];

@@ -314,3 +314,52 @@ def test_phased_uneven_batch_chunked_graph_and_oracle():
         assert np.abs(one["final"][b] - ref[-1]).max() <= 1e-12
         assert np.abs(one["readout"][b, :n] - ref @ w).max() <= 1e-12
         assert np.all(one["readout"][b, n:] == 0.0)
+
+
+def test_register_state_variant_matches_row_parts():
+    """Variant 5 (the row-part layout with the state in registers, moved by
+    warp shuffles) against variant 4 (state in shared memory): the same
+    arithmetic in the same order, so the same numbers (up to the sign of a
+    zero) -- on a uniform NV-7 sweep, an uneven phased batch and a table
+    run -- and the oracle."""
+    from superspinsim_gb300 import protocols
+    from superspinsim_gb300.sweep import Sweep, population_weights
+    c = load_case("nv7_n49")
+    gens, vm = c["generators"], c["vectorisation_map"]
+    f_res = 2.870e9 + 28.025e9*5e-3
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1
+    w = population_weights(vm, [3, 4, 5])
+    dt, F = 1e-9, 40
+    freqs = f_res + np.linspace(-20e6, 20e6, 300)
+    progs = np.zeros((len(freqs), 4, 1, 5))
+    progs[:, :, :, 0] = np.inf
+    progs[:, 0, 0, 2] = 5e6/28.025e9
+    progs[:, 0, 0, 3] = freqs
+    progs[:, 3, 0, 1] = 10/65.9
+    rng = np.random.default_rng(4)
+    B = 2600
+    rprogs, dur = protocols.ramsey(rng.uniform(40e6, 80e6, B), rng.uniform(-5e6, 5e6, B),
+                                   rng.uniform(0, 20e-9, B), f_res, 10/65.9, t_init=4e-9,
+                                   t_read=3e-9)
+    samples = np.ceil(dur/dt).astype(np.int32)
+    Tr = int(samples.max())
+    out = {}
+    for variant in (4, 5):
+        sw = Sweep(gens, vm, number_of_exponentials=2, number_of_fine_divisions=F,
+                   variant=variant)
+        a = sw.run(rho, progs, 0.0, 6*dt + 1e-13, dt, readout_weights=w, final_state=True)
+        assert sw.info()["lanes"] == 32
+        b = sw.run(rho, rprogs, 0.0, Tr*dt + 1e-13, dt, samples=samples, readout_weights=w,
+                   final_state=True)
+        out[variant] = (a, b)
+    for k in ("readout", "final"):
+        assert np.array_equal(out[4][0][k], out[5][0][k])
+        assert np.array_equal(out[4][1][k], out[5][1][k])
+    a = out[5][0]
+    W, nodes = quadrature(2)
+    _, ref = oracle.simulate(gens, np.stack([rho]*3), 0.0, 6*dt + 1e-13, dt, progs[[0, 150, 299]],
+                             K=2, W=W, nodes=nodes, F=F, vectorisation_map=vm, mode="vector",
+                             degree=16, flat_out=True)
+    assert np.abs(a["final"][[0, 150, 299]] - ref[:, -1]).max() <= 1e-12
+    assert np.abs(a["readout"][[0, 150, 299]] - ref @ w).max() <= 1e-12
