@@ -344,14 +344,6 @@ static int batch_run_impl(sss_plan* p, int ntraj, const double* rho0, int nch, i
             d_tr = p->w_out.as<double>();
         }
     }
-    // reachability needs rho0's support on the host
-    std::vector<double> h_rho0((size_t)ntraj * N);
-    if (host) {
-        memcpy(h_rho0.data(), rho0, sizeof(double) * h_rho0.size());
-    } else {
-        SSS_CUDA(cudaMemcpy(h_rho0.data(), rho0, sizeof(double) * h_rho0.size(), cudaMemcpyDeviceToHost));
-    }
-    (void)h_rho0;
     int rc = batch_run(p, ntraj, d_rho0, nch, nseg, tab ? nullptr : d_prog, d_samples,
                        samples ? h_samples.data() : nullptr, t0, dt, T_max, F, readout_weights,
                        d_ro, d_fin, st, d_tr, d_tab);
