@@ -307,16 +307,85 @@ static int run_reference(const oracle_desc* d, double t0, double dt, int T,
 
 /* ---- vector mode -------------------------------------------------------- */
 
+/* The exponent on the union pattern of the generators (entries that are
+ * zero in every generator are zero in every exponent): row_ptr (N+1) and
+ * col (nnz, increasing within a row).  Skipping exact zeros leaves every
+ * sum of the dense forms unchanged (up to the sign of a zero result). */
+typedef struct {
+    int nnz;
+    int* row_ptr;
+    int* col;
+} oracle_pattern;
+
+static int build_pattern(const oracle_desc* d, oracle_pattern* pt) {
+    int N = d->N, planes = d->rotating ? d->Q * d->G : d->G;
+    pt->row_ptr = (int*)malloc((size_t)(N + 1) * sizeof(int));
+    pt->col = (int*)malloc((size_t)N * N * sizeof(int));
+    if (!pt->row_ptr || !pt->col) return -1;
+    int nnz = 0;
+    for (int y = 0; y < N; y++) {
+        pt->row_ptr[y] = nnz;
+        for (int x = 0; x < N; x++) {
+            int any = 0;
+            for (int g = 0; g < planes && !any; g++)
+                any = d->gens[((size_t)g * N + y) * N + x] != 0.0;
+            if (any) pt->col[nnz++] = x;
+        }
+    }
+    pt->row_ptr[N] = nnz;
+    pt->nnz = nnz;
+    return 0;
+}
+
+/* build_exponent restricted to the pattern: val[p] = Omega[y][col[p]],
+ * formed with the same operations in the same order */
+static void build_exponent_sparse(const oracle_desc* d, const oracle_pattern* pt,
+                                  const double* coef, int e, double h, double* val) {
+    int N = d->N, G = d->G, Q = d->Q;
+    if (!d->rotating) {
+        double wc[16];
+        for (int g = 0; g < G; g++) {
+            double acc = 0;
+            for (int k = 0; k < Q; k++) acc += d->W[e * Q + k] * coef[k * G + g];
+            wc[g] = acc;
+        }
+        for (int y = 0; y < N; y++)
+            for (int p = pt->row_ptr[y]; p < pt->row_ptr[y + 1]; p++) {
+                int x = pt->col[p];
+                double acc = 0.0;
+                for (int g = 0; g < G; g++)
+                    acc += wc[g] * d->gens[((size_t)g * N + y) * N + x];
+                val[p] = h * acc;
+            }
+    } else {
+        for (int y = 0; y < N; y++)
+            for (int p = pt->row_ptr[y]; p < pt->row_ptr[y + 1]; p++) {
+                int x = pt->col[p];
+                double acc = 0;
+                for (int k = 0; k < Q; k++)
+                    for (int g = 0; g < G; g++) {
+                        double m0 = d->gens[(((size_t)k * G + g) * N + y) * N + x] *
+                                    coef[k * G + g];
+                        double m1 = h * d->W[e * Q + k];
+                        acc += m0 * m1;
+                    }
+                val[p] = acc;
+            }
+    }
+}
+
 /* v <- exp(Om) v by Taylor series of the given degree (residual form:
- * the increment sum_{j>=1} Om^j v / j! is added to v at the end). */
-static void expv(const double* Om, double* v, int N, int degree, double* term,
-                 double* next, double* incr) {
+ * the increment sum_{j>=1} Om^j v / j! is added to v at the end); Om on
+ * the pattern. */
+static void expv(const oracle_pattern* pt, const double* val, double* v, int N, int degree,
+                 double* term, double* next, double* incr) {
     memcpy(term, v, N * sizeof(double));
     for (int i = 0; i < N; i++) incr[i] = 0.0;
     for (int j = 1; j <= degree; j++) {
         for (int y = 0; y < N; y++) {
             double acc = 0.0;
-            for (int k = 0; k < N; k++) acc += Om[y * N + k] * term[k];
+            for (int p = pt->row_ptr[y]; p < pt->row_ptr[y + 1]; p++)
+                acc += val[p] * term[pt->col[p]];
             next[y] = acc / j;
         }
         for (int i = 0; i < N; i++) incr[i] += next[i];
@@ -331,9 +400,13 @@ static int run_vector(const oracle_desc* d, double t0, double dt, int T,
                       int F, const double* rho0, double* out) {
     int N = d->N, G = d->G, K = d->K, Q = d->Q;
     size_t NN = (size_t)N * N;
+    oracle_pattern pt = {0, NULL, NULL};
     double* Om = (double*)malloc(NN * sizeof(double));
     double* v = (double*)malloc(5 * N * sizeof(double));
-    if (!Om || !v) { free(Om); free(v); return -1; }
+    if (!Om || !v || build_pattern(d, &pt)) {
+        free(Om); free(v); free(pt.row_ptr); free(pt.col);
+        return -1;
+    }
     double *term = v + N, *next = v + 2 * N, *incr = v + 3 * N, *tmp = v + 4 * N;
     double coef[64];
     memcpy(v, rho0, N * sizeof(double));
@@ -346,8 +419,8 @@ static int run_vector(const oracle_desc* d, double t0, double dt, int T,
                 sample_row(d->prog, d->nseg, d->nch, !d->rotating, tn, coef + k * G, G);
             }
             for (int e = K - 1; e >= 0; e--) {
-                build_exponent(d, coef, e, h, Om);
-                expv(Om, v, N, d->degree, term, next, incr);
+                build_exponent_sparse(d, &pt, coef, e, h, Om);
+                expv(&pt, Om, v, N, d->degree, term, next, incr);
             }
             if (d->rotating) {
                 /* v <- e^{L0 h} v with the residual-aware blocks */
@@ -373,6 +446,8 @@ static int run_vector(const oracle_desc* d, double t0, double dt, int T,
     }
     free(Om);
     free(v);
+    free(pt.row_ptr);
+    free(pt.col);
     return 0;
 }
 
