@@ -51,7 +51,9 @@ extern "C" {
 #define SSS_EINVAL (-1)     /* bad shape or argument */
 #define SSS_ENOMEM (-2)     /* device or host allocation failed */
 #define SSS_ECUDA (-3)      /* a CUDA call failed */
-#define SSS_ETIMEOUT (-4)   /* a device wait ran out of iterations */
+#define SSS_ETIMEOUT (-4)   /* a device wait ran out of iterations (reserved:
+                               no kernel of this library waits on a flag --
+                               the work queue is a bare atomic counter) */
 #define SSS_ENONFINITE (-5) /* a state became NaN or infinite */
 #define SSS_ENODEVICE (-6)  /* no CUDA device */
 
