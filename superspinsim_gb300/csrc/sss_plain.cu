@@ -543,13 +543,14 @@ int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
 //
 // Some callers cannot allocate device memory: code running inside another
 // framework's memory pool (which would fragment or be bypassed), callers
-// on a device whose memory is already fully reserved, or callers in a
-// context where allocation is forbidden (for example while a caller-managed
-// CUDA graph is being built).  sss_simulate_noalloc runs the same two
-// kernels as sss_simulate_device for one trajectory in the lab frame, but
-// instead of a plan's buffers it uses one file-scope device array as its
-// scratch: the weight/node table, the chain's running state and a chunk of
-// step propagators.  It allocates nothing on the device or the host.
+// on a device whose memory is already fully reserved, or callers whose own
+// rules forbid allocation while they run.  sss_simulate_noalloc runs the
+// same two kernels as sss_simulate_device for one trajectory in the lab
+// frame, but instead of a plan's buffers it uses one file-scope device
+// array as its scratch: the weight/node table, the chain's running state
+// and a chunk of step propagators.  It allocates nothing on the device or
+// the host, and it copies nothing from host memory: the weight/node table
+// reaches the scratch as a kernel argument.
 //
 // Limits: N <= 52 (the shared-memory path), lab frame only, and the
 // step-propagator chunk must hold at least one N x N matrix (always true
@@ -557,9 +558,10 @@ int plain_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
 // keeps it until the process exits.  Every call shares it and it keeps the
 // last call's contents, so calls that overlap on the GPU (on different
 // streams, or from different host threads) race and corrupt each other.
-// The first call on a device looks up the array's device address and sets
-// the kernel's shared-memory limit on that device; make that first call
-// before any stream capture.
+// The first call on a device looks up the array's device address on that
+// device; make that first call before any stream capture.  Every call sets
+// the step kernel's shared-memory limit for its own N (other entry points
+// of the library set the same per-function limit for theirs).
 // ---------------------------------------------------------------------------
 
 namespace sss {
@@ -588,14 +590,21 @@ int noalloc_scratch(double** out) {
         void* ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-        e = cudaFuncSetAttribute(k_step_propagators, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(8 * (size_t)kPlainMaxN * kPlainMaxN * sizeof(double)));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
         d.ptr = static_cast<double*>(ptr);
         d.ready = true;
     }
     *out = d.ptr;
     return SSS_OK;
+}
+
+// The CF weights (K*Q) then the nodes (Q), passed by value.
+struct NoallocTable {
+    double v[kMaxK * kMaxQ + kMaxQ];
+    int n;
+};
+
+__global__ void k_noalloc_table(const NoallocTable t, double* __restrict__ dst) {
+    for (int i = threadIdx.x; i < t.n; i += blockDim.x) dst[i] = t.v[i];
 }
 
 }  // namespace
@@ -639,12 +648,17 @@ extern "C" int sss_simulate_noalloc(const sss_plan_desc* d, const double* genera
     const int chunk = (int)std::min<size_t>((size_t)T, prop_capacity);
 
     cudaStream_t st = (cudaStream_t)stream;
-    double host_wn[32];
-    for (int i = 0; i < d->K * d->Q; i++) host_wn[i] = weights[i];
-    for (int k = 0; k < d->Q; k++) host_wn[d->K * d->Q + k] = nodes[k];
-    SSS_CUDA(cudaMemcpyAsync(wn, host_wn, sizeof(double) * (d->K * d->Q + d->Q),
-                             cudaMemcpyHostToDevice, st));
+    NoallocTable tbl{};
+    tbl.n = d->K * d->Q + d->Q;
+    for (int i = 0; i < d->K * d->Q; i++) tbl.v[i] = weights[i];
+    for (int k = 0; k < d->Q; k++) tbl.v[d->K * d->Q + k] = nodes[k];
+    k_noalloc_table<<<1, 32, 0, st>>>(tbl, wn);
+    SSS_CUDA(cudaGetLastError());
+    // the limit is per function and per device, and the plan entry points
+    // set it for their own N, so it is set here on every call
     const size_t smem = 8 * NN * sizeof(double);
+    SSS_CUDA(cudaFuncSetAttribute(k_step_propagators, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
     for (int t_begin = 0; t_begin < T; t_begin += chunk) {
         int Tc = std::min(chunk, T - t_begin);
         PlainArgs a{};
