@@ -213,9 +213,12 @@ int sss_batch_launch(sss_plan* plan, double* state, const double* programs,
  * decay rate, trapezoid weights over the readout window) and its gradient
  * with respect to the amplitude and phase of every segment of channel 0
  * (the x field):  grad[(b*nseg + s)*2 + 0] = dJ/d amplitude_s,
- * grad[(b*nseg + s)*2 + 1] = dJ/d phase_s.  Forward pass with
- * sqrt(T*F)-step checkpoints, then a backward sweep that recomputes each
- * interval; the exponential's derivative is exact for the truncated series
+ * grad[(b*nseg + s)*2 + 1] = dJ/d phase_s.  The forward pass stores the
+ * state before every exponential (trajectories in chunks that fit the
+ * memory bound of sss_plan_set_adjoint_memory) and the backward sweep walks
+ * them back; when the states of one trajectory do not fit, a checkpointed
+ * sweep (about sqrt(T*F) checkpoints, each interval recomputed) runs
+ * instead.  The exponential's derivative is exact for the truncated series
  * the forward pass uses.  Lab frame.  readout_weights (N) and time_weights
  * (T) are host arrays; the rest follow `host` as in sss_batch_run. */
 int sss_adjoint_run(sss_plan* plan, int ntraj, const double* rho0, int nch,

@@ -94,25 +94,50 @@ typedef struct {
 
 /* ---- dense helpers, in the reference's loop order ---------------------- */
 
-/* out = (res ? 2*in : 0) + in@in   (generate_simulator.py:706-724) */
-static void square_mat(const double* in, double* out, int N, int res) {
+/* Column-major copy of a right operand, so the inner products below read
+ * both operands contiguously.  The products and their summation order are
+ * unchanged (k ascending), so results are bit for bit those of the
+ * row-major loops. */
+static double* transposed(const double* m, int N) {
+    double* t = (double*)malloc((size_t)N * N * sizeof(double));
+    if (!t) return NULL;
+    for (int k = 0; k < N; k++)
+        for (int x = 0; x < N; x++) t[(size_t)x * N + k] = m[(size_t)k * N + x];
+    return t;
+}
+
+/* out = (res ? 2*in : 0) + in@in   (generate_simulator.py:706-724).
+ * Returns -1 if the scratch copy cannot be allocated. */
+static int square_mat(const double* in, double* out, int N, int res) {
+    double* it = transposed(in, N);
+    if (!it) return -1;
     for (int y = 0; y < N; y++)
         for (int x = 0; x < N; x++) {
+            const double* a = in + (size_t)y * N;
+            const double* b = it + (size_t)x * N;
             double acc = res ? 2 * in[y * N + x] : 0.0;
-            for (int k = 0; k < N; k++) acc += in[y * N + k] * in[k * N + x];
+            for (int k = 0; k < N; k++) acc += a[k] * b[k];
             out[y * N + x] = acc;
         }
+    free(it);
+    return 0;
 }
 
 /* out = (res ? L + R : 0) + L@R   (generate_simulator.py:726-743) */
-static void mul_mat(const double* L, const double* Rm, double* out, int N,
-                    int res) {
+static int mul_mat(const double* L, const double* Rm, double* out, int N,
+                   int res) {
+    double* rt = transposed(Rm, N);
+    if (!rt) return -1;
     for (int y = 0; y < N; y++)
         for (int x = 0; x < N; x++) {
+            const double* a = L + (size_t)y * N;
+            const double* b = rt + (size_t)x * N;
             double acc = res ? L[y * N + x] + Rm[y * N + x] : 0.0;
-            for (int k = 0; k < N; k++) acc += L[y * N + k] * Rm[k * N + x];
+            for (int k = 0; k < N; k++) acc += a[k] * b[k];
             out[y * N + x] = acc;
         }
+    free(rt);
+    return 0;
 }
 
 /* Rotating-frame step, TE <- e^{L0 h} TE, residual aware
@@ -234,18 +259,25 @@ static int run_reference(const oracle_desc* d, double t0, double dt, int T,
                         if (!d->residual)
                             for (int i = 0; i < N; i++) O[i * N + i] += 1.0;
                         for (int q = 0; q < d->R; q++) {
-                            square_mat(O, sc, N, d->residual);
-                            square_mat(sc, O, N, d->residual);
+                            if (square_mat(O, sc, N, d->residual) ||
+                                square_mat(sc, O, N, d->residual)) {
+#pragma omp atomic write
+                                bad = 1;
+                            }
                         }
                     }
                     double* te = TE + t * NN;
                     /* :1259-1294 -- exponential K-1 first, 0 last */
                     for (int e = 0; e < K; e += 2) {
-                        mul_mat(Om + (K - e - 1) * NN, te, sc, N, d->residual);
+                        int rc = mul_mat(Om + (K - e - 1) * NN, te, sc, N, d->residual);
                         if (e + 1 < K)
-                            mul_mat(Om + (K - e - 2) * NN, sc, te, N, d->residual);
+                            rc |= mul_mat(Om + (K - e - 2) * NN, sc, te, N, d->residual);
                         else
                             memcpy(te, sc, NN * sizeof(double));
+                        if (rc) {
+#pragma omp atomic write
+                            bad = 1;
+                        }
                     }
                     if (d->rotating) {
                         apply_eig(d, te, sc2);
@@ -266,7 +298,11 @@ static int run_reference(const oracle_desc* d, double t0, double dt, int T,
     double* sc = (double*)malloc(NN * sizeof(double));
     if (!sc) { free(TE); return -1; }
     for (int t = 0; t + 1 < T; t++) {
-        mul_mat(TE + (t + 1) * NN, TE + t * NN, sc, N, d->residual);
+        if (mul_mat(TE + (t + 1) * NN, TE + t * NN, sc, N, d->residual)) {
+            free(sc);
+            free(TE);
+            return -1;
+        }
         memcpy(TE + (t + 1) * NN, sc, NN * sizeof(double));
     }
     free(sc);

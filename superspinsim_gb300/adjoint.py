@@ -3,7 +3,12 @@
 ``sss_adjoint_run`` (libsss.so) computes, for a batch of trajectories, the
 objective J = sum_t tw[t] * rw . rho(t) -- e.g. integrated fluorescence --
 and its gradient with respect to the amplitude and phase of every segment
-of the x-drive channel, by a checkpointed adjoint sweep on the GPU.
+of the x-drive channel, by an adjoint sweep on the GPU: the forward pass
+stores the state before every exponential when device memory allows it
+(trajectories in memory-sized chunks) and the backward pass walks the
+stored states; when one trajectory's states do not fit, a checkpointed
+sweep (about sqrt(steps) checkpoints, each interval recomputed) runs
+instead.
 ``PulseObjective`` exposes it to torch.autograd: piecewise-constant pulse
 amplitudes (Rabi frequency, Hz) and phases (rad) in, objective out.
 """

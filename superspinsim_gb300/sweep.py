@@ -219,15 +219,29 @@ class ChunkedRun:
         return self
 
     def save(self, path):
-        """Checkpoint: the device state, the next sample index and the
-        readouts so far."""
-        np.savez(path, state=self.state.cpu().numpy(), t_next=self.t_next,
-                 readout=None if self.readout is None else self.readout.cpu().numpy())
+        """Checkpoint: the device state, the next sample index, the batch
+        shape and the readouts so far (omitted when the run has none)."""
+        arrays = {"state": self.state.cpu().numpy(), "t_next": self.t_next,
+                  "shape": np.array([self.B, self.N, self.T_max])}
+        if self.readout is not None:
+            arrays["readout"] = self.readout.cpu().numpy()
+        np.savez(path, **arrays)
 
     def load(self, path):
-        with np.load(path, allow_pickle=True) as z:
+        """Resume from a checkpoint written by save() for a batch of the same
+        shape (plain arrays only: no pickled objects are read)."""
+        with np.load(path, allow_pickle=False) as z:
+            shape = tuple(int(v) for v in z["shape"])
+            if shape != (self.B, self.N, self.T_max):
+                raise ValueError(f"checkpoint is for (B, N, T_max) = {shape}, this run is "
+                                 f"{(self.B, self.N, self.T_max)}")
+            if (self.readout is not None) != ("readout" in z.files):
+                raise ValueError("checkpoint and run disagree on whether readouts are kept")
+            t_next = int(z["t_next"])
+            if not 0 <= t_next <= self.T_max:
+                raise ValueError(f"checkpoint sample index {t_next} out of range")
             self.state.copy_(self.torch.from_numpy(z["state"]))
-            self.t_next = int(z["t_next"])
+            self.t_next = t_next
             if self.readout is not None:
                 self.readout.copy_(self.torch.from_numpy(z["readout"]))
         return self

@@ -1,8 +1,9 @@
 """Generate the golden fixtures under ``tests/golden/`` from the reference.
 
 This script is test infrastructure.  It imports the unmodified reference
-package (monashNV/superspinsim 1.3.2) from ``$SSS_REFERENCE`` (default
-``/root/reference``) and runs its own CPU path.  numba and qutip are not
+package (monashNV/superspinsim 1.3.2) from the checkout named by the
+environment variable ``SSS_REFERENCE`` (required) and runs its own CPU
+path.  numba and qutip are not
 installed here, so a small import shim stands in for them:
 
 * ``numba.jit`` becomes the identity and ``numba.prange`` becomes ``range``
@@ -28,9 +29,14 @@ project's segment format, and the density operators returned by
 window.  Where the case is one of the reference's golden regression tests,
 the leading values of its CSV (``test/reference/*.csv``) are stored too.
 
-Run:  python tests/golden/make_golden.py            (about 5 minutes, 1 core)
+Run:  SSS_REFERENCE=<reference checkout> python tests/golden/make_golden.py
+                                                    (about 5 minutes, 1 core)
       python tests/golden/make_golden.py modes      (unitary / kernel mode arrays)
       python tests/golden/make_golden.py csv        (the golden CSVs in full)
+      python tests/golden/make_golden.py fullrun    (full-length runs of the
+          reference's algorithm through the oracle's reference mode: NV-7
+          over 400,000 steps, NV-21 over 104; about 30 minutes on 8 cores;
+          no reference checkout needed)
 """
 import math
 import os
@@ -40,7 +46,7 @@ import time as _time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get("SSS_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("SSS_REFERENCE")
 
 _SHIM = {
     "numba/__init__.py": (
@@ -115,6 +121,9 @@ def install_shim():
         os.makedirs(os.path.dirname(path), exist_ok=True)
         with open(path, "w") as f:
             f.write(text)
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "superspinsim")):
+        raise SystemExit("set SSS_REFERENCE to a checkout of monashNV/superspinsim 1.3.2 "
+                         "(the directory that holds superspinsim/)")
     sys.path.insert(0, REFERENCE)
     sys.path.insert(0, root)
 
@@ -513,9 +522,92 @@ def save_quadratures():
     np.savez(os.path.join(HERE, "quadratures.npz"), **arrays)
 
 
+# Full-length runs of the reference's algorithm -----------------------------
+# The oracle's reference mode reproduces the reference's simulate bit for
+# bit on every fixture above (tests/test_oracle_golden.py), so it stands in
+# for the reference on runs far too long for the shimmed Python: the whole
+# 400,000-step NV-7 ODMR trajectory and a 104-step window of the NV-21
+# (441 x 441) sweep.  Both use the reference's own generators (the nv7_n49
+# and nv21_n441 fixtures) and its quadrature tables (quadratures.npz); they
+# need no reference checkout.
+
+F_RES_NV7 = 2.870e9 + 28.025e9*5e-3
+F_RES_NV21 = 2.870e9 + 28.025e9*0.05
+
+
+def odmr_program(freq, rabi=5e6, laser=10/65.9):
+    """x drive of Rabi frequency `rabi` at `freq`, laser pumping at `laser`
+    of saturation, for all time (the ODMR workloads' programs)."""
+    p = np.zeros((4, 1, 5))
+    p[:, :, 0] = np.inf
+    p[0, 0, 2:4] = [rabi/28.025e9, freq]
+    p[3, 0, 1] = laser
+    return p
+
+
+def _flat(rho, vm):
+    out = np.zeros(vm.shape[0])
+    for i, (y, x, c) in enumerate(vm):
+        out[i] = rho[y, x].imag if c else rho[y, x].real
+    return out
+
+
+def save_fullruns(which=("nv7_fullrun", "nv21_window")):
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle import oracle
+    with np.load(os.path.join(HERE, "quadratures.npz")) as z:
+        W, nodes = z["weights_4_2_gl"], z["samples_2_gl"]
+    if "nv7_fullrun" in which:
+        # the 1024-frequency sweep's trajectory 512 (the one nearest the
+        # ms=0 -> +1 line), 2 us at 5 ps: T = 2000 samples of 1 ns, F = 200
+        with np.load(os.path.join(HERE, "nv7_n49.npz")) as z:
+            gens, vm = z["generators"], z["vectorisation_map"]
+        freqs = F_RES_NV7 + np.linspace(-30e6, 30e6, 1024)
+        index = 512
+        prog = odmr_program(freqs[index])
+        rho = np.zeros((7, 7), complex)
+        rho[1, 1] = 1.0
+        T, dt, F = 2000, 1e-9, 200
+        t = _time.time()
+        _, out = oracle.simulate(gens, rho, 0.0, T*dt + 1e-13, dt, prog, K=2, W=W, nodes=nodes,
+                                 F=F, vectorisation_map=vm, mode="reference", flat_out=True)
+        w = np.zeros(vm.shape[0])
+        for i, (y, x, c) in enumerate(vm):
+            if y == x and c == 0 and y in (3, 4, 5):
+                w[i] = 65.9e6
+        keep = np.arange(99, T, 100)
+        np.savez_compressed(os.path.join(HERE, "nv7_fullrun.npz"), index=index,
+                            freqs=freqs, program=prog, rho0=_flat(rho, vm), T=T, dt=dt, F=F,
+                            fluorescence=out @ w, readout_weights=w, kept_samples=keep,
+                            states=out[keep])
+        print(f"nv7_fullrun: {T*F} steps in {_time.time() - t:.0f} s", flush=True)
+    if "nv21_window" in which:
+        # four trajectories of the 256-frequency NV-21 sweep, 8 samples of
+        # 65 ps with F = 13 (104 steps of 5 ps), every sample's state kept
+        with np.load(os.path.join(HERE, "nv21_n441.npz")) as z:
+            gens, vm = z["generators"], z["vectorisation_map"]
+        freqs = F_RES_NV21 + np.linspace(-30e6, 30e6, 256)
+        index = np.array([0, 100, 128, 255])
+        progs = np.stack([odmr_program(freqs[i]) for i in index])
+        rho = np.zeros((21, 21), complex)
+        for k in range(3, 6):
+            rho[k, k] = 1/3
+        T, dt, F = 8, 65e-12, 13
+        t = _time.time()
+        _, out = oracle.simulate(gens, np.stack([rho]*len(index)), 0.0, T*dt + 1e-15, dt, progs,
+                                 K=2, W=W, nodes=nodes, F=F, vectorisation_map=vm,
+                                 mode="reference", flat_out=True)
+        np.savez_compressed(os.path.join(HERE, "nv21_window.npz"), index=index, freqs=freqs,
+                            programs=progs, rho0=_flat(rho, vm), T=T, dt=dt, F=F, states=out)
+        print(f"nv21_window: {len(index)} x {T*F} steps in {_time.time() - t:.0f} s", flush=True)
+
+
 def main():
-    install_shim()
     only = set(sys.argv[1:])
+    if only & {"nv7_fullrun", "nv21_window", "fullrun"}:
+        save_fullruns(tuple(only) if "fullrun" not in only else ("nv7_fullrun", "nv21_window"))
+        return
+    install_shim()
     if "modes" in only:
         save_modes()
         return
