@@ -270,7 +270,15 @@ int sss_plan_last_launches(const sss_plan* plan);
  * small patterns only -- SSS_EINVAL when the pattern does not fit; 5 = as
  * 4, with the state in registers moved by warp shuffles where the layout
  * allows it: 32 lanes, one chain per lane, no lane owning two rows, lab
- * frame).  No
+ * frame; 6 = slot-packed: every lane runs the same S FMA slots per Horner
+ * term in scaled Horner form (the v term of a row is one more entry), rows
+ * of n entries taking n + 1 slots with no padding to a part length
+ * (sss_slot_layout), 8 to 256 lanes, up to 16 slots; 7 = phased row parts:
+ * per lane C1 chains of P1 slots, a barrier, then C2 chains of P2 slots
+ * that start from parked partial sums, every chain starting at a fixed
+ * slot, 8, 16 or 32 lanes).  Automatic lanes: per lane count the cheapest
+ * layout (FP64 instructions per Horner term), and the lane count whose
+ * busiest SM sub-partition issues the fewest of them.  No
  * reference counterpart (the reference's launch shapes are fixed,
  * generate_simulator.py:85-106). */
 int sss_plan_set_batch_config(sss_plan* plan, int lanes, int cta_threads,
@@ -291,6 +299,26 @@ int sss_plan_set_adjoint_memory(sss_plan* plan, size_t max_bytes);
  * NULL. */
 int sss_plan_batch_info(const sss_plan* plan, int* lanes, int* degree,
                         int* substeps, int* rows, int* nnz, double* kernel_ms);
+
+/* Layout utility (no reference counterpart; host only, needs no device):
+ * the slot-packed layout that batched runs use (variant 6) for a row
+ * pattern of M rows, row i holding columns col[row_ptr[i] .. row_ptr[i+1])
+ * (state rows of Omega's non-zeros), at `lanes` lanes per trajectory (8 to
+ * 256) and at most max_slots slots per lane (capped at 16).  Every lane runs
+ * the same `slots` FMA instructions per Horner term: a row of n entries
+ * takes n entry slots and one close slot (its v term), and a row cut
+ * between two lanes parks a partial sum before slot `barrier_slot` (equal
+ * to `slots` when no row is cut) that the other lane picks up there or
+ * later.  words and entries (16*lanes values each, [slot*lanes + lane])
+ * receive each slot's word -- bits 0-13 the state row it reads (an entry; a
+ * partial index for a partial add) or closes (a close), bit 14 partial add,
+ * bit 15 close, bit 16 piece start, bit 17 start from partial `pidx`, bit
+ * 18 park the sum as partial `pidx`, bits 19-31 pidx -- and the index into
+ * col of the entry it multiplies (-1: close or padding, -2: partial add).
+ * SSS_EINVAL when no layout of at most max_slots slots exists. */
+int sss_slot_layout(int M, const int* row_ptr, const int* col, int lanes,
+                    int max_slots, int* slots, int* barrier_slot, int* partials,
+                    unsigned* words, int* entries);
 
 /* Measurement utility (no reference counterpart): FP64 FMA throughput of
  * the current device in TFLOP/s, from a bounded DFMA loop (8 independent

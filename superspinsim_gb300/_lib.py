@@ -26,7 +26,7 @@ SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
            "sss_plan_set_projection", "sss_plan_set_unitary",
            "sss_fp64_peak", "sss_fp64_mma_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
-           "sss_batch_prepare_samples", "sss_batch_launch", "sss_last_error",
+           "sss_batch_prepare_samples", "sss_batch_launch", "sss_slot_layout", "sss_last_error",
            "sss_plan_destroy"]
 
 
@@ -95,6 +95,9 @@ def load(build_if_missing=True):
         L.sss_batch_launch.argtypes = [vp, vp, vp, vp, d, i, i, i, vp, vp]
         L.sss_batch_launch.restype = i
         L.sss_fp64_peak.restype = i
+        L.sss_slot_layout.argtypes = [i, ip, ip, i, i, ip, ip, ip,
+                                      ctypes.POINTER(ctypes.c_uint), ip]
+        L.sss_slot_layout.restype = i
         L.sss_last_error.restype = ctypes.c_char_p
         L.sss_plan_destroy.argtypes = [vp]
         L.sss_plan_destroy.restype = None
@@ -349,3 +352,27 @@ def fp64_mma_peak_tflops(stream=None):
     v = ctypes.c_double()
     check(load().sss_fp64_mma_peak(ctypes.byref(v), stream))
     return v.value
+
+
+SLOTS_MAX = 16
+
+
+def slot_layout(row_ptr, col, lanes, max_slots=SLOTS_MAX):
+    """The slot-packed layout of a row pattern (sss_slot_layout; host only).
+    Returns (slots, barrier_slot, partials, words (slots, lanes) uint32,
+    entries (slots, lanes) int: index into col, -1 close/padding, -2
+    partial add)."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    M = row_ptr.size - 1
+    words = np.zeros(SLOTS_MAX*lanes, dtype=np.uint32)
+    entries = np.zeros(SLOTS_MAX*lanes, dtype=np.int32)
+    S, bar, npart = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    ip = ctypes.POINTER(ctypes.c_int)
+    check(load().sss_slot_layout(
+        M, row_ptr.ctypes.data_as(ip), col.ctypes.data_as(ip), int(lanes), int(max_slots),
+        ctypes.byref(S), ctypes.byref(bar), ctypes.byref(npart),
+        words.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), entries.ctypes.data_as(ip)))
+    n = S.value
+    return (n, bar.value, npart.value, words.reshape(SLOTS_MAX, lanes)[:n].copy(),
+            entries.reshape(SLOTS_MAX, lanes)[:n].copy())

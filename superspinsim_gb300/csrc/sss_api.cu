@@ -468,6 +468,12 @@ int sss_batch_launch(sss_plan* p, double* state, const double* programs, const i
 
 int sss_plan_last_launches(const sss_plan* p) { return p ? p->last_launches : 0; }
 
+int sss_slot_layout(int M, const int* row_ptr, const int* col, int lanes, int max_slots,
+                    int* slots, int* barrier_slot, int* partials, unsigned* words, int* entries) {
+    return sss::slot_layout_host(M, row_ptr, col, lanes, max_slots, slots, barrier_slot, partials,
+                                 words, entries);
+}
+
 // FP64 FMA throughput probe: every thread runs 8 independent DFMA chains.
 static __global__ void k_dfma_peak(double* out, int iters, double a, double b) {
     double x[8];
@@ -562,11 +568,12 @@ int sss_plan_set_batch_config(sss_plan* p, int lanes, int cta_threads, int varia
     if (!p) return fail(SSS_EINVAL, "null plan");
     if (lanes < 0 || lanes > 256 || (lanes & (lanes - 1)))
         return fail(SSS_EINVAL, "lanes must be 0 (automatic) or a power of two up to 256");
-    if (lanes > 32 && variant != 0 && variant != 4)
-        return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part variant");
+    if (lanes > 32 && variant != 0 && variant != 4 && variant != 6)
+        return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part or "
+                                "slot-packed variant");
     if (cta_threads != 0 && (cta_threads < 32 || cta_threads > 256 || cta_threads % 32))
         return fail(SSS_EINVAL, "cta_threads must be 0 or a multiple of 32 in [32, 256]");
-    if (variant < 0 || variant > 5) return fail(SSS_EINVAL, "variant must be 0, 1, 2, 3, 4 or 5");
+    if (variant < 0 || variant > 7) return fail(SSS_EINVAL, "variant must be 0 to 7");
     p->batch_lanes = lanes;
     p->batch_threads = cta_threads;
     p->batch_variant = variant;

@@ -43,8 +43,10 @@
 #include <cmath>
 #include <functional>
 #include <numeric>
+#include <random>
 #include <vector>
 
+#include "sss_batch_args.cuh"
 #include "sss_device.cuh"
 #include "sss_internal.cuh"
 
@@ -95,60 +97,7 @@ int build_sparse(sss_plan* p) {
 
 namespace {
 
-constexpr int kMaxTaylor = 24;
 
-struct BatchArgs {
-    int M;        // state rows kept (reachable)
-    int Ga;       // active generators
-    int K, Q, F, nch, nseg, T_max, ntraj, degree, substeps, N;
-    int E;        // entries per lane (max over lanes)
-    int t_begin, t_end;        // output samples of this launch
-    double h_sub, t0, dt;
-    int gen_index[kMaxSlots];  // active generator -> coefficient slot
-    const double* toff;        // F: (r*dt)/F
-    const double* noff;        // Q: (dt*node_k)/F
-    const double* W;           // K*Q
-    const double* gv;          // Ga * E * L  generator values [g][e][l]
-    const unsigned* ent;       // E * L  packed entry words [e][l]
-    const int* lane_rows;      // L: entries of each lane
-    const int* rbeg;           // L+1: rows [rbeg[l], rbeg[l+1]) belong to lane l
-    const int* row_orig;       // M
-    const double* rw;          // M readout weights (or null)
-    const double* rho0;        // ntraj*N  state at sample t_begin
-    const double* prog;        // ntraj*nch*nseg*5
-    const int* samples;        // ntraj or null
-    double* readout;           // ntraj*T_max or null
-    double* fin;               // ntraj*N  state after the launch (may alias rho0), or null
-    double* trace;             // ntraj*T_max*N  state after every output sample, or null
-    int* queue;
-    // row-part variant
-    const int* pcol;           // C*P*L  column of each part entry [e][l] (M: the zero row)
-    const unsigned* cw;        // kCloseMax*L  close words [k][l]
-    const double* om0;         // K*C*P*L  constant part of Omega per exponential
-    int kc;                    // close slots per lane (max over lanes)
-    int n_live;                // generators assembled per step (the others are in om0)
-    int live[kMaxSlots];       // their active-generator slots
-    int live_k[kMaxSlots];     // node of a rotating slot (weight W[e,k] c_k), -1: sum over nodes
-    int live_ch[kMaxSlots];    // index of its channel among the live channels
-    int n_lch;                 // live channels (sampled into the ring)
-    int lch_chan[kMaxSlots];   // their program channel (>= nch: zero)
-    // generalised rotating frame (state in the eigenbasis of L0)
-    int rot, resid;
-    const double* Vm;          // N*N eigenvectors (lab = V x)
-    const double* Vinvm;       // N*N inverse (x = V^-1 rho)
-    const double* blk_self;    // M: e^{L0 h} diagonal coefficient of each row (minus 1 when residual)
-    const double* blk_part;    // M: coefficient of its partner row
-    const int* blk_pos;        // M: the partner's row (M: none, the zero row)
-    const int* order;          // ntraj: queue position -> trajectory (longest first), or null
-    // coefficient table instead of programs (row-part kernel): per trajectory
-    // F*T_max*Q rows of tab_G values, row (r*T_max + t)*Q + k for node k of
-    // fine step r of output sample t; a slot's channel is its table column
-    const double* tab;
-    int tab_G;
-    double* states;            // state before every exponential, or null:
-    long st_steps;             //   [((b*st_steps + n)*K + e)*M + row], n = step since t_begin
-    double inv_j[kMaxTaylor + 1];
-};
 
 // Entry word: bits 0-15 column (compressed), bits 16-31 (row + 1) when the
 // entry closes its row, else 0.
@@ -962,40 +911,6 @@ __global__ void __launch_bounds__(256, 1) k_batch_shfl(const BatchArgs a) {
     }
 }
 
-template <class Kern>
-int launch(sss_plan* p, Kern kern, const BatchArgs& a, int threads, int slots_per_cta,
-           size_t smem, cudaStream_t st) {
-    SSS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    SSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
-    if (per_sm < 1) return fail(SSS_EINVAL, "batched kernel does not fit on an SM");
-    // one group per trajectory with work in this launch (at most as many as
-    // fit): every group then starts on a trajectory of its own and the CTAs
-    // spread evenly over the SMs (a grid sized for trajectories that only
-    // pad their readout would leave the working ones wherever the queue
-    // happened to hand them out)
-    const int n_work = p->launch_active > 0 ? std::min(p->launch_active, a.ntraj) : a.ntraj;
-    int want = (n_work + slots_per_cta - 1) / slots_per_cta;
-    int grid = std::max(1, std::min(want, per_sm * p->num_sms));
-    // the launch's own timing events, except while the stream is being
-    // captured into a graph (events recorded there cannot be waited on)
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    SSS_CUDA(cudaStreamIsCapturing(st, &cap));
-    const bool timed = cap == cudaStreamCaptureStatusNone;
-    if (timed && !p->ev_begin) {
-        SSS_CUDA(cudaEventCreate(&p->ev_begin));
-        SSS_CUDA(cudaEventCreate(&p->ev_end));
-    }
-    if (timed && !p->ev_keep_begin) SSS_CUDA(cudaEventRecord(p->ev_begin, st));
-    kern<<<grid, threads, smem, st>>>(a);
-    SSS_CUDA(cudaGetLastError());
-    if (timed) {
-        SSS_CUDA(cudaEventRecord(p->ev_end, st));
-        p->ev_recorded = true;
-    }
-    p->last_grid = grid;
-    return SSS_OK;
-}
 
 
 template <int L>
@@ -1211,6 +1126,422 @@ int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::En
     return SSS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Slot-packed layout (k_batch_slots with SlotProgram).
+//
+// Rows are laid lane after lane in lanes of S slots by McNaughton's
+// wrap-around rule for preemptive scheduling (McNaughton, Management
+// Science 6(1), 1959): a row of n entries takes n + 1 consecutive slots (its
+// entries, then its v entry, whose slot stores the row), and a row that
+// crosses a lane boundary is cut in two -- its first entries at the start
+// of the next lane (a donor, which parks its partial sum) and the rest at
+// the end of this lane (a receiver, which starts from that partial sum).
+// Donors end by the barrier slot SA = S/2 and receivers start at SA or
+// later, so one barrier per Horner term orders them; the cut costs no
+// instruction.  A row longer than S first hands entries to standalone
+// donors at lane starts (from the last lane back, inside [0, SA)); its own
+// piece adds each of their partial sums with one more slot after SA.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct SlotCell {
+    int kind = 0;  // 0 padding, 1 entry, 2 partial add, 3 the row's v entry
+    int row = -1, ent = -1, part = -1, pidx = 0;
+    int store_row = -1;  // the row this slot's sum completes (stored to the next iterate)
+    unsigned flags = 0;
+};
+
+bool slots_try(const std::vector<int>& nent, const std::vector<int>& order, int L, int S, int SA,
+               std::vector<SlotCell>& cell, int* npart_out) {
+    cell.assign((size_t)L * S, SlotCell{});
+    auto at = [&](int l, int q) -> SlotCell& { return cell[(size_t)l * S + q]; };
+    const bool bar = SA >= 1 && SA < S;
+    int npart = 0;
+    struct Item { int row, e0, n; std::vector<int> adds; };
+    struct Don { int row, e0, n, pidx; };
+    std::vector<Item> items;
+    std::vector<Don> dons;
+    for (int i : order) {
+        const int n = nent[i];
+        if (n + 1 <= S) {
+            items.push_back({i, 0, n, {}});
+            continue;
+        }
+        if (!bar) return false;
+        int taken = 0;
+        std::vector<int> adds;
+        while ((n - taken) + (int)adds.size() + 1 > S) {
+            const int k = std::min(SA, n - taken);
+            if (k <= 0) return false;
+            dons.push_back({i, taken, k, npart});
+            adds.push_back(npart++);
+            taken += k;
+        }
+        items.push_back({i, taken, n - taken, adds});
+    }
+    auto put_donor = [&](int row, int e0, int n, int l, int q0, int pidx) {
+        for (int k = 0; k < n; k++) {
+            SlotCell& c = at(l, q0 + k);
+            c.kind = 1;
+            c.row = row;
+            c.ent = e0 + k;
+            if (k == 0) c.flags |= kSlotStart;
+            if (k == n - 1) {
+                c.flags |= kSlotDend;
+                c.pidx = pidx;
+            }
+        }
+    };
+    auto put_closer = [&](int row, int e0, int n, const std::vector<int>& adds, int l, int q0,
+                          int recv) {
+        int q = q0;
+        for (int k = 0; k < n; k++, q++) {
+            SlotCell& c = at(l, q);
+            c.kind = 1;
+            c.row = row;
+            c.ent = e0 + k;
+        }
+        for (int pa : adds) {
+            SlotCell& c = at(l, q++);
+            c.kind = 2;
+            c.row = row;
+            c.part = pa;
+        }
+        SlotCell& c = at(l, q);
+        c.kind = 3;
+        c.row = row;
+        c.store_row = row;
+        SlotCell& f = at(l, q0);
+        f.flags |= kSlotStart;
+        if (recv >= 0) {
+            f.flags |= kSlotRecv;
+            f.pidx = recv;
+        }
+    };
+    std::vector<int> reserve(L, 0);
+    {
+        int l = L - 1;
+        for (const Don& d : dons) {
+            while (l >= 0 && reserve[l] + d.n > SA) l--;
+            if (l < 0) return false;
+            put_donor(d.row, d.e0, d.n, l, reserve[l], d.pidx);
+            reserve[l] += d.n;
+        }
+    }
+    int lane = 0, pos = reserve[0];
+    for (const Item& it : items) {
+        const int m = (int)it.adds.size();
+        const int n = it.n + m + 1;
+        while (true) {
+            if (lane >= L) return false;
+            if (pos + n <= S && (m == 0 || pos + it.n >= SA)) {  // whole, adds after the barrier
+                put_closer(it.row, it.e0, it.n, it.adds, lane, pos, -1);
+                pos += n;
+                if (pos == S) {
+                    lane++;
+                    pos = lane < L ? reserve[lane] : 0;
+                }
+                break;
+            }
+            // cut: receiver [pos, S) here, donor at the start of the next lane
+            const int recv_ents = S - pos - 1 - m;
+            const int a = it.n - recv_ents;
+            if (bar && recv_ents >= 0 && pos >= SA && a >= 1 && lane + 1 < L &&
+                reserve[lane + 1] + a <= SA) {
+                const int pidx = npart++;
+                put_closer(it.row, it.e0 + a, recv_ents, it.adds, lane, pos, pidx);
+                put_donor(it.row, it.e0, a, lane + 1, reserve[lane + 1], pidx);
+                lane++;
+                pos = reserve[lane] + a;
+                break;
+            }
+            lane++;  // pad the rest of this lane
+            pos = lane < L ? reserve[lane] : 0;
+        }
+    }
+    *npart_out = npart;
+    return true;
+}
+
+// Smallest compiled S (up to S_cap) with a slot layout of rows of nent
+// entries on L lanes: S from the lower bound ceil(sum(n+1)/L) up, with no cut
+// first, then the barrier at S/2, each with the rows in decreasing size and
+// then in seeded random orders; the first layout that fits wins.
+bool slots_pack(const std::vector<int>& nent, int L, int S_cap, std::vector<SlotCell>& cell,
+                int* S_out, int* SA_out, int* npart_out) {
+    const int M = (int)nent.size();
+    long total = 0;
+    for (int n : nent) total += n + 1;
+    const int lo = (int)std::max<long>(1, (total + L - 1) / L);
+    std::vector<int> base(M);
+    std::iota(base.begin(), base.end(), 0);
+    std::stable_sort(base.begin(), base.end(), [&](int x, int y) { return nent[x] > nent[y]; });
+    const int tries = std::max(8, std::min(4000, 60000 / std::max(1, M)));
+    for (int s = lo; s <= std::min(S_cap, kSlotsMax); s++) {
+        if (!slot_size_compiled(s)) continue;
+        for (int sa : {s, s / 2}) {
+            if (sa < 1) continue;
+            std::mt19937 rng(1234567u + 31u * s + sa);
+            std::vector<int> ord = base;
+            for (int t = 0; t < (sa == s ? 2 : tries); t++) {
+                if (t > 0) std::shuffle(ord.begin(), ord.end(), rng);
+                int np = 0;
+                if (slots_try(nent, ord, L, s, sa, cell, &np) && np < (1 << (32 - kSlotPidxShift))) {
+                    *S_out = s;
+                    *SA_out = sa;
+                    *npart_out = np;
+                    return true;
+                }
+            }
+        }
+    }
+    return false;
+}
+
+// Phased row-part layout (k_batch_slots with PhasedProgram).  A row of n
+// entries is n + 1 items (its entries and its v entry).  Per lane, phase 1
+// runs C1 chains of P1 slots and phase 2 runs C2 chains of P2 slots; every
+// chain starts at a fixed slot (phase 1 from zero, phase 2 from a parked
+// partial sum or zero), so no lane needs a per-slot choice of start value.
+// A row is one of
+//   * one phase-1 chain (n + 1 <= P1), which stores the row;
+//   * one phase-2 chain (n + 1 <= P2), from zero;
+//   * k phase-1 chains (parts) and one phase-2 chain that starts from the
+//     first part's partial sum, adds the other k - 1 partial sums (one slot
+//     each) and the r items left, (k - 1) + r <= P2.
+// Rows take the option with the fewest phase-1 chains; chains are dealt to
+// lanes round-robin.
+bool phased_pack(const std::vector<int>& nent, int L, const PhasedShape& sh, std::vector<SlotCell>& cell,
+                 int* npart_out) {
+    const int M = (int)nent.size();
+    const int C1 = sh.C1, P1 = sh.P1, C2 = sh.C2, P2 = sh.P2;
+    const int S1 = C1 * P1, S = S1 + C2 * P2;
+    cell.assign((size_t)L * S, SlotCell{});
+    struct Choice { int k, r; };
+    std::vector<Choice> plan(M);
+    long n1 = 0, n2 = 0;
+    for (int i = 0; i < M; i++) {
+        const int n = nent[i] + 1;
+        if (n <= P1) {
+            plan[i] = {1, 0};
+            n1 += 1;
+            continue;
+        }
+        if (n <= P2) {
+            plan[i] = {0, n};
+            n2 += 1;
+            continue;
+        }
+        int k = 1;
+        for (;; k++) {
+            const int rmax = P2 - (k - 1);
+            if (rmax < 0) return false;
+            if (n - rmax <= k * P1) break;
+        }
+        plan[i] = {k, std::max(0, n - k * P1)};
+        n1 += k;
+        n2 += 1;
+    }
+    if (n1 > (long)C1 * L || n2 > (long)C2 * L) return false;
+    auto at = [&](int l, int q) -> SlotCell& { return cell[(size_t)l * S + q]; };
+    // items of a row: its entries 0..n-1, then its v entry
+    auto put_item = [&](SlotCell& c, int row, int it) {
+        c.row = row;
+        if (it < nent[row]) {
+            c.kind = 1;
+            c.ent = it;
+        } else {
+            c.kind = 3;
+        }
+    };
+    int j1 = 0, j2 = 0, npart = 0;
+    for (int i = 0; i < M; i++) {
+        const Choice& pl = plan[i];
+        const int n = nent[i] + 1;
+        const bool single = pl.k == 1 && pl.r == 0;
+        int it = 0;
+        std::vector<int> parts;
+        for (int k = 0; k < pl.k; k++) {
+            const int left = (n - pl.r) - it;
+            const int len = k == pl.k - 1 ? left : std::min(P1, left);
+            const int lane = j1 % L, ch = j1 / L;
+            j1++;
+            for (int e = 0; e < len; e++) put_item(at(lane, e * C1 + ch), i, it++);
+            SlotCell& last = at(lane, (P1 - 1) * C1 + ch);
+            if (single) {
+                last.store_row = i;
+            } else {
+                last.flags |= kSlotDend;
+                last.pidx = npart;
+                parts.push_back(npart++);
+            }
+        }
+        if (single) continue;
+        const int lane = j2 % L, ch = j2 / L;
+        j2++;
+        int e = 0;
+        if (!parts.empty()) {
+            SlotCell& f = at(lane, S1 + ch);
+            f.flags |= kSlotRecv;
+            f.pidx = parts[0];
+        }
+        for (size_t pp = 1; pp < parts.size(); pp++, e++) {
+            SlotCell& c = at(lane, S1 + e * C2 + ch);
+            c.kind = 2;
+            c.row = i;
+            c.part = parts[pp];
+        }
+        for (; it < n; it++, e++) {
+            if (e >= P2) return false;
+            put_item(at(lane, S1 + e * C2 + ch), i, it);
+        }
+        at(lane, S1 + (P2 - 1) * C2 + ch).store_row = i;
+    }
+    *npart_out = npart;
+    return true;
+}
+
+}  // namespace
+
+// Kernel tables of a slot-cell layout (S slots x L lanes, cell [l*S + q]):
+// rows owned by the lane that stores them, renumbered in lane order; load
+// words [q][l], then store words [S + q][l] (partial sum p lives at row
+// M+2+p of the next iterate); generator values and entry indices per slot
+// (entry_q -2 marks a partial add, an entry of coefficient 1).
+static int emit_slot_cells(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows,
+                           const std::vector<SlotCell>& cell, int L, int S, int npart,
+                           const std::vector<int>& active, const std::vector<int>& rows_reached,
+                           BatchLayout& Ly) {
+    const SparseGenerators& sp = p->sparse;
+    const int M = (int)rows.size(), Ga = (int)active.size();
+    std::vector<std::vector<int>> own(L);
+    for (int l = 0; l < L; l++)
+        for (int q = 0; q < S; q++)
+            if (cell[(size_t)l * S + q].store_row >= 0) own[l].push_back(cell[(size_t)l * S + q].store_row);
+    for (auto& o : own) std::sort(o.begin(), o.end());
+    std::vector<int>& newpos = Ly.newpos;
+    std::vector<int>& row_orig = Ly.row_orig;
+    newpos.assign(M, -1);
+    row_orig.assign(M, 0);
+    {
+        int k = 0;
+        for (int l = 0; l < L; l++)
+            for (int i : own[l]) {
+                if (newpos[i] >= 0) return fail(SSS_EINVAL, "slot layout stores a row twice");
+                newpos[i] = k;
+                row_orig[k] = rows_reached[i];
+                k++;
+            }
+        if (k != M) return fail(SSS_EINVAL, "slot layout lost a row");
+    }
+    if (M + 2 + npart > (int)kSlotIdx)
+        return fail(SSS_EINVAL, "slot layout: rows plus partial sums exceed 16381");
+    const unsigned zero_row = (unsigned)M, sink = (unsigned)M + 1;
+    Ly.cw.assign((size_t)2 * S * L, 0u);
+    Ly.entry_q.assign((size_t)S * L, -1);
+    Ly.gv.assign((size_t)Ga * S * L, 0.0);
+    for (int l = 0; l < L; l++)
+        for (int q = 0; q < S; q++) {
+            const SlotCell& c = cell[(size_t)l * S + q];
+            const size_t idx = (size_t)q * L + l;
+            unsigned ld = zero_row, st = sink, base = zero_row;
+            if (c.kind == 1) {
+                const BatchLayout::Ent& en = rows[c.row][c.ent];
+                ld = (unsigned)newpos[en.col];
+                Ly.entry_q[idx] = en.q;
+                for (int gi = 0; gi < Ga; gi++)
+                    Ly.gv[((size_t)gi * S + q) * L + l] = sp.val[(size_t)active[gi] * sp.nnz + en.q];
+            } else if (c.kind == 2) {
+                ld = kLdNext | (unsigned)(M + 2 + c.part);
+                Ly.entry_q[idx] = -2;
+            } else if (c.kind == 3) {
+                ld = kLdV | (unsigned)newpos[c.row];
+            }
+            if (c.store_row >= 0) st = (unsigned)newpos[c.store_row];
+            if (c.flags & kSlotDend) st = (unsigned)(M + 2 + c.pidx);
+            if (c.flags & kSlotRecv) base = (unsigned)(M + 2 + c.pidx);
+            const bool start = c.kind == 0 || (c.flags & kSlotStart);
+            Ly.cw[idx] = ld;
+            Ly.cw[(size_t)S * L + idx] = st | (base << 14) | (start ? kStStart : 0u);
+        }
+    Ly.pcol.clear();
+    Ly.lane_of = own;
+    return SSS_OK;
+}
+
+static void set_slot_fields(BatchLayout& Ly, int L, int S, int SA, int npart, int threads) {
+    Ly.parts = true;
+    Ly.slots = true;
+    Ly.C = 1;
+    Ly.P = S;
+    Ly.kc = 0;
+    Ly.S = S;
+    Ly.bar_at = SA;
+    Ly.npart = npart;
+    Ly.L = L;
+    Ly.E = S;
+    Ly.use_reg = false;
+    Ly.epl = 0;
+    Ly.threads = threads;
+}
+
+// Slot-packed layout at L lanes with at most S_cap slots; SSS_EINVAL when
+// none fits.
+int slots_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows, int L,
+                      int threads, int S_cap, const std::vector<int>& active,
+                      const std::vector<int>& rows_reached, BatchLayout* out) {
+    BatchLayout& Ly = *out;
+    const int M = (int)rows.size();
+    if (L != 8 && L != 16 && L != 32 && L != 64 && L != 128 && L != 256)
+        return fail(SSS_EINVAL, "slot-packed variant needs 8 to 256 lanes per trajectory (a power of two)");
+    if (L > 32) threads = L;
+    if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
+    if (M + 2 > (int)kSlotIdx) return fail(SSS_EINVAL, "slot-packed variant supports at most 16381 rows");
+    std::vector<int> nent(M);
+    for (int i = 0; i < M; i++) nent[i] = (int)rows[i].size();
+    std::vector<SlotCell> cell;
+    int S = 0, SA = 0, npart = 0;
+    if (!slots_pack(nent, L, S_cap, cell, &S, &SA, &npart))
+        return fail(SSS_EINVAL, "slot-packed variant does not fit this pattern at " + std::to_string(L) +
+                                    " lanes per trajectory");
+    if (int rc = emit_slot_cells(p, rows, cell, L, S, npart, active, rows_reached, Ly)) return rc;
+    set_slot_fields(Ly, L, S, SA, npart, threads);
+    Ly.phased = false;
+    return SSS_OK;
+}
+
+// Phased row-part layout at L lanes: the first shape of kPhasedShapes (in
+// order of slots per lane, at most S_cap) that fits.
+int phased_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows, int L,
+                       int threads, int S_cap, const std::vector<int>& active,
+                       const std::vector<int>& rows_reached, BatchLayout* out) {
+    BatchLayout& Ly = *out;
+    const int M = (int)rows.size();
+    if (L != 8 && L != 16 && L != 32)
+        return fail(SSS_EINVAL, "phased row-part variant needs 8, 16 or 32 lanes per trajectory");
+    if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
+    if (M + 2 > (int)kSlotIdx) return fail(SSS_EINVAL, "phased row-part variant supports at most 16381 rows");
+    std::vector<int> nent(M);
+    for (int i = 0; i < M; i++) nent[i] = (int)rows[i].size();
+    std::vector<SlotCell> cell;
+    int best = -1, npart = 0;
+    for (int k = 0; k < kPhasedShapeCount && best < 0; k++) {
+        const PhasedShape& sh = kPhasedShapes[k];
+        if (sh.C1 * sh.P1 + sh.C2 * sh.P2 > S_cap) continue;
+        if (phased_pack(nent, L, sh, cell, &npart)) best = k;
+    }
+    if (best < 0)
+        return fail(SSS_EINVAL, "phased row-part variant does not fit this pattern at " +
+                                    std::to_string(L) + " lanes per trajectory");
+    const PhasedShape& sh = kPhasedShapes[best];
+    const int S = sh.C1 * sh.P1 + sh.C2 * sh.P2;
+    if (int rc = emit_slot_cells(p, rows, cell, L, S, npart, active, rows_reached, Ly)) return rc;
+    set_slot_fields(Ly, L, S, sh.C1 * sh.P1, npart, threads);
+    Ly.phased = true;
+    Ly.shape = best;
+    return SSS_OK;
+}
+
 // Per column of a coefficient table (rows x G): the largest |value|, the
 // smallest and largest value, and a count of non-finite values; one partial
 // per CTA in out[(cta*G + g)*4 + {0,1,2,3}], reduced on the host.
@@ -1293,6 +1624,37 @@ static int table_stats(sss_plan* p, const double* d_tab, size_t rows, int G, std
         chval[g] = rows > 0 ? lo : 0.0;
     }
     return SSS_OK;
+}
+
+// FP64 instructions per Horner term of one group: C*P + kc for the row-part
+// layout, S for the slot-packed and phased ones; a group wider than a warp
+// pays about half an instruction per CTA barrier.
+static double layout_cost(const BatchLayout& Ly) {
+    double c = Ly.slots ? Ly.S : Ly.C * Ly.P + Ly.kc;
+    if (Ly.L > 32) c += 0.5 * (Ly.slots ? (Ly.bar_at < Ly.S ? 2 : 1) : 2);
+    return c;
+}
+
+// Automatic lane count for n trajectories, from the cost of the best layout
+// at each lane count 8, 16, ..., 256 (0: does not fit): the count whose
+// busiest SM sub-partition issues the fewest FP64 instructions per Horner
+// term, ceil(warps / sub-partitions) * cost; ties go to the wider group (more
+// warps to hide latency).  0 when nothing fits.
+int auto_lanes(const sss_plan* p, const double* cost, long n) {
+    int best = 0;
+    double best_v = 0.0;
+    const long subparts = 4L * p->num_sms;
+    for (int i = 0; i < kLaneCounts; i++) {
+        if (cost[i] <= 0.0) continue;
+        const long Lc = 8L << i;
+        const long warps = (std::max(1L, n) * Lc + 31) / 32;
+        const double v = (double)((warps + subparts - 1) / subparts) * cost[i];
+        if (!best || v <= best_v) {
+            best = (int)Lc;
+            best_v = v;
+        }
+    }
+    return best;
 }
 
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
@@ -1478,47 +1840,93 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
     // while the batch gives at most two warps per SM sub-partition, else 16
     // (two trajectories per warp, fewer instructions per trajectory)
     const bool parts_asked = p->batch_variant == 4 || p->batch_variant == 5;
-    if (rot && !force_parts && allow_register && p->batch_variant != 0 && !parts_asked)
-        return fail(SSS_EINVAL, "the rotating frame runs on the row-part kernel (variant 0 or 4)");
-    if (table && !force_parts && p->batch_variant != 0 && !parts_asked)
-        return fail(SSS_EINVAL, "a coefficient table runs on the row-part kernel (variant 0 or 4)");
-    if (force_parts || (allow_register && (rot || table || parts_asked ||
-                                           p->batch_variant == 0))) {
-        // lanes: as configured, or the narrowest group (fewest instructions
-        // per trajectory) that still gives every SM sub-partition a warp and
-        // whose pattern fits; else the widest that fits
+    const bool slots_asked = p->batch_variant == 6;
+    const bool phased_asked = p->batch_variant == 7;
+    const bool row_kernels = parts_asked || slots_asked || phased_asked;
+    const bool slots_ok = !force_parts && (p->batch_variant == 0 || slots_asked);
+    const bool phased_ok = !force_parts && (p->batch_variant == 0 || phased_asked);
+    const bool parts_ok = force_parts || (!slots_asked && !phased_asked);
+    if (rot && !force_parts && allow_register && p->batch_variant != 0 && !row_kernels)
+        return fail(SSS_EINVAL, "the rotating frame runs on the row-part, slot-packed or phased "
+                                "kernel (variant 0, 4, 6 or 7)");
+    if (table && !force_parts && p->batch_variant != 0 && !row_kernels)
+        return fail(SSS_EINVAL, "a coefficient table runs on the row-part, slot-packed or phased "
+                                "kernel (variant 0, 4, 6 or 7)");
+    if (force_parts || (allow_register && (rot || table || row_kernels || p->batch_variant == 0))) {
         const int threads_cfg = p->batch_threads > 0 ? p->batch_threads : 32;
-        int rc = SSS_EINVAL;
-        if (p->batch_lanes > 0 && !force_parts) {
-            rc = parts_layout_rows(p, Ly.row_ents, {}, L, threads_cfg, 1, 1, active, rows_reached,
-                                   out, nullptr);
-        } else {
-            int chosen = 0;
-            long parts4 = 0;  // parts of at most 4 entries: lanes beyond twice that stay idle
-            for (const auto& re : Ly.row_ents) parts4 += std::max<long>(1, ((long)re.size() + 3) / 4);
-            for (int Lc : {8, 16, 32, 64, 128, 256}) {
-                if (chosen && Lc > 2 * parts4) break;
-                BatchLayout trial;
-                trial.row_ents = Ly.row_ents;
-                if (parts_layout_rows(p, trial.row_ents, {}, Lc, threads_cfg, 1, 1, active,
-                                      rows_reached, &trial, nullptr) != SSS_OK)
-                    continue;
-                chosen = Lc;
-                const long n_rule = p->auto_lanes_ntraj > 0 ? p->auto_lanes_ntraj : ntraj;
-                if (n_rule * Lc >= 4L * 32 * p->num_sms) break;
+        // At Lc lanes: the cheapest of the row-part (0), phased row-part (1)
+        // and slot-packed (2) layouts that fit (FP64 instructions per Horner
+        // term, layout_cost); ties go to the earlier one (the phased
+        // layout's fixed chain starts beat the slot-packed layout's per-slot
+        // start selects at equal slots).  The layout functions write only
+        // the layout fields of their output.
+        auto best_at = [&](int Lc, bool fill) {
+            double cost[3] = {0.0, 0.0, 0.0};
+            int cap[3] = {0, 0, 0};
+            BatchLayout t;
+            if (parts_ok && parts_layout_rows(p, Ly.row_ents, {}, Lc, threads_cfg, 1, 1, active,
+                                              rows_reached, &t, nullptr) == SSS_OK)
+                cost[0] = layout_cost(t);
+            auto cap_below = [](double c) { return c > 0.0 ? (int)std::ceil(c) - 1 : 64; };
+            cap[1] = cap_below(cost[0]);
+            if (phased_ok && Lc <= 32 && cap[1] >= 1) {
+                BatchLayout tq;
+                if (phased_layout_rows(p, Ly.row_ents, Lc, threads_cfg, cap[1], active, rows_reached,
+                                       &tq) == SSS_OK)
+                    cost[1] = layout_cost(tq);
             }
-            if (chosen)
-                rc = parts_layout_rows(p, Ly.row_ents, {}, chosen, threads_cfg, 1, 1, active,
-                                       rows_reached, out, nullptr);
-            else
-                fail(SSS_EINVAL, "row-part variant does not fit this pattern");
+            double lim = 0.0;
+            for (double c : {cost[0], cost[1]})
+                if (c > 0.0 && (lim == 0.0 || c < lim)) lim = c;
+            cap[2] = std::min(kSlotsMax, cap_below(lim));
+            if (slots_ok && cap[2] >= 1) {
+                BatchLayout ts;
+                if (slots_layout_rows(p, Ly.row_ents, Lc, threads_cfg, cap[2], active, rows_reached,
+                                      &ts) == SSS_OK)
+                    cost[2] = layout_cost(ts);
+            }
+            int pick = -1;
+            for (int k = 0; k < 3; k++)
+                if (cost[k] > 0.0 && (pick < 0 || cost[k] < cost[pick])) pick = k;
+            if (pick < 0) return 0.0;
+            if (fill) {
+                int r = SSS_EINVAL;
+                if (pick == 0)
+                    r = parts_layout_rows(p, Ly.row_ents, {}, Lc, threads_cfg, 1, 1, active,
+                                          rows_reached, out, nullptr);
+                else if (pick == 1)
+                    r = phased_layout_rows(p, Ly.row_ents, Lc, threads_cfg, cap[1], active,
+                                           rows_reached, out);
+                else
+                    r = slots_layout_rows(p, Ly.row_ents, Lc, threads_cfg, cap[2], active,
+                                          rows_reached, out);
+                if (r != SSS_OK) return 0.0;
+            }
+            return cost[pick];
+        };
+        // lanes as configured, or the automatic count (auto_lanes)
+        int rc = SSS_EINVAL, chosen = 0;
+        if (p->batch_lanes > 0 && !force_parts) {
+            chosen = L;
+        } else {
+            const long n_rule = p->auto_lanes_ntraj > 0 ? p->auto_lanes_ntraj : ntraj;
+            for (int i = 0; i < kLaneCounts; i++) p->auto_cost[i] = best_at(8 << i, false);
+            chosen = auto_lanes(p, p->auto_cost, n_rule);
+        }
+        if (chosen && best_at(chosen, true) > 0.0) {
+            rc = SSS_OK;
+        } else {
+            const char* what = slots_asked ? "slot-packed" : phased_asked ? "phased row-part" : "row-part";
+            rc = chosen ? fail(SSS_EINVAL, std::string(what) + " variant does not fit this pattern at " +
+                                               std::to_string(chosen) + " lanes per trajectory")
+                        : fail(SSS_EINVAL, std::string(what) + " variant does not fit this pattern");
         }
         if (rc == SSS_OK) {
             Ly.nnz = nnz;
             Ly.degree = degree;
             Ly.substeps = substeps;
         }
-        if (rc == SSS_OK || parts_asked || force_parts || rot || table) return rc;
+        if (rc == SSS_OK || row_kernels || force_parts || rot || table) return rc;
     }
     if (L > 32)
         return fail(SSS_EINVAL, "more than 32 lanes per trajectory needs the row-part variant, "
@@ -1682,6 +2090,11 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
                 }
             }
         }
+        // slot layouts: a partial add is an entry of coefficient 1
+        if (Ly.slots)
+            for (int e = 0; e < p->d.K; e++)
+                for (int i = 0; i < CP * L; i++)
+                    if (Ly.entry_q[i] == -2) om0[(size_t)e * CP * L + i] = 1.0;
         dbl.insert(dbl.end(), om0.begin(), om0.end());
     }
     const size_t n_gv = dbl.size();
@@ -1767,6 +2180,27 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
         a.n_lch = (int)lch.size();
         for (size_t i = 0; i < lch.size(); i++) a.lch_chan[i] = lch[i];
     }
+    if (Ly.slots) {
+        a.S = Ly.S;
+        a.bar_at = Ly.bar_at;
+        a.npart = Ly.npart;
+        // per live generator, the slots where some lane holds a non-zero value
+        for (size_t i = 0; i < live.size(); i++) {
+            unsigned m = 0;
+            for (int q = 0; q < Ly.S; q++)
+                for (int l = 0; l < L; l++)
+                    if (Ly.gv[((size_t)live[i] * Ly.S + q) * L + l] != 0.0) m |= 1u << q;
+            a.amask[i] = m;
+        }
+        // scaled Horner coefficients c_j = d!/(j-1)! = j (j+1) ... d, and 1/d!
+        for (int j = 0; j <= kMaxTaylor; j++) a.cfac[j] = 0.0;
+        for (int j = 1; j <= degree; j++) {
+            double c = 1.0;
+            for (int k = j; k <= degree; k++) c *= k;
+            a.cfac[j] = c;
+        }
+        a.inv_dfact = 1.0 / a.cfac[1];
+    }
     a.rot = rot ? 1 : 0;
     a.resid = (p->d.flags & SSS_RESIDUAL) ? 1 : 0;
     if (rot) {
@@ -1784,7 +2218,11 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
     for (int j = 0; j <= kMaxTaylor; j++) a.inv_j[j] = j ? 1.0 / j : 0.0;
 
     *out = a;
-    if (Ly.parts) {
+    if (Ly.slots) {
+        const size_t per_slot = (3 * (size_t)(M + 2 + Ly.npart) +
+                                 (size_t)kRing * (p->d.Q * lch.size() + p->d.K * live.size())) | 1;
+        *smem = sizeof(double) * ((threads / L) * per_slot + M);
+    } else if (Ly.parts) {
         const size_t per_slot = (3 * (size_t)(M + 2) + L * Ly.C + 1 +
                                  (size_t)kRing * (p->d.Q * lch.size() + p->d.K * live.size())) | 1;
         *smem = sizeof(double) * ((threads / L) * per_slot + M);
@@ -1857,7 +2295,8 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
     // shorter chains per trajectory).  A launch switches layout at those
     // samples, as a chunked run switches chunks.
     const bool phased = h_samples && ntraj > 1 && p->batch_lanes == 0 &&
-                        (p->batch_variant == 0 || p->batch_variant == 4 || p->batch_variant == 5);
+                        (p->batch_variant == 0 || p->batch_variant == 4 || p->batch_variant == 5 ||
+                         p->batch_variant == 6 || p->batch_variant == 7);
     if (phased) {
         p->batch_longest.assign(h_samples, h_samples + ntraj);
         std::sort(p->batch_longest.begin(), p->batch_longest.end(), std::greater<int>());
@@ -1893,11 +2332,15 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
         ph.use_reg = Ly.use_reg;
         ph.one_chain = p->batch_variant == 3;
         ph.parts = Ly.parts;
+        ph.slots = Ly.slots;
+        ph.phased = Ly.phased;
+        ph.S = Ly.S;
+        ph.shape = Ly.shape;
         // the register-state form: one trajectory per warp, one chain per
         // lane, no lane owning two rows, and a lane whose parts are all
         // padding (the zero partial of the padding close slots); lab frame
         ph.shfl = false;
-        if (p->batch_variant == 5 && Ly.parts && Ly.L == 32 && Ly.C == 1 && !p->rotating) {
+        if (p->batch_variant == 5 && Ly.parts && !Ly.slots && Ly.L == 32 && Ly.C == 1 && !p->rotating) {
             bool ok = true, pad_lane = false;
             for (int l = 0; l < Ly.L && ok; l++) ok = Ly.lane_of[l].size() <= 1;
             for (int l = 0; l < Ly.L && !pad_lane; l++) {
@@ -1916,12 +2359,20 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
             p->last_nnz = (int)Ly.nnz;
             p->last_epl = Ly.E;
             p->last_active = Ly.Ga;
-            p->last_variant = Ly.parts ? 4 : Ly.use_reg ? (ph.one_chain ? 3 : 1) : 2;
+            p->last_variant = Ly.phased ? 7 : Ly.slots ? 6 : Ly.parts ? 4 : Ly.use_reg ? (ph.one_chain ? 3 : 1) : 2;
         }
         if (!phased || !Ly.parts) break;
-        const long thr = (4L * 32 * p->num_sms + Ly.L - 1) / Ly.L;
-        if (thr > ntraj || p->batch_longest[thr - 1] <= t) break;
-        t = p->batch_longest[thr - 1];
+        // the next phase starts at the first sample where the automatic
+        // lane count for the trajectories still running changes
+        const int n_now = running_after(p, t);
+        int n_next = -1;
+        for (int n = n_now - 1; n >= 1; n--)
+            if (auto_lanes(p, p->auto_cost, n) != Ly.L) {
+                n_next = n;
+                break;
+            }
+        if (n_next < 0 || p->batch_longest[n_next] <= t) break;
+        t = p->batch_longest[n_next];
     }
     p->batch_ready = true;
     return SSS_OK;
@@ -1985,6 +2436,10 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
         if (ph.shfl) {
             rc = ph.P == 4 ? launch(p, k_batch_shfl<4>, a, threads, threads / 32, smem, st)
                            : launch(p, k_batch_shfl<8>, a, threads, threads / 32, smem, st);
+        } else if (ph.phased) {
+            rc = launch_phased(p, L, ph.shape, a, threads, smem, st);
+        } else if (ph.slots) {
+            rc = launch_slots(p, L, ph.S, a, threads, smem, st);
         } else if (ph.parts) {
             switch (L) {
                 case 8: rc = launch_parts<8>(p, ph.C, ph.P, a, threads, smem, st); break;
@@ -2068,6 +2523,51 @@ int parts_forward_launch(sss_plan* p, const PartsForward& fw, int ntraj, double*
         case 128: return launch_parts<128>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
         default: return launch_parts<256>(p, fw.C, fw.P, a, fw.threads, fw.smem, st);
     }
+}
+
+int slot_layout_host(int M, const int* row_ptr, const int* col, int L, int S_cap, int* S_out,
+                     int* bar_out, int* npart_out, unsigned* words, int* entries) {
+    if (M < 0 || M + 2 > (int)kSlotIdx || !row_ptr || !S_out || !bar_out || !npart_out || !words ||
+        !entries)
+        return fail(SSS_EINVAL, "bad slot layout arguments");
+    if (L != 8 && L != 16 && L != 32 && L != 64 && L != 128 && L != 256)
+        return fail(SSS_EINVAL, "lanes must be 8, 16, 32, 64, 128 or 256");
+    std::vector<int> nent(M);
+    for (int i = 0; i < M; i++) {
+        nent[i] = row_ptr[i + 1] - row_ptr[i];
+        if (nent[i] < 0) return fail(SSS_EINVAL, "row_ptr must not decrease");
+        for (int k = row_ptr[i]; k < row_ptr[i + 1]; k++)
+            if (!col || col[k] < 0 || col[k] >= M) return fail(SSS_EINVAL, "column out of range");
+    }
+    std::vector<SlotCell> cell;
+    int S = 0, SA = 0, np = 0;
+    if (!slots_pack(nent, L, std::min(S_cap, kSlotsMax), cell, &S, &SA, &np))
+        return fail(SSS_EINVAL, "no slot layout up to the given number of slots");
+    for (int q = 0; q < kSlotsMax; q++)
+        for (int l = 0; l < L; l++) {
+            const size_t o = (size_t)q * L + l;
+            words[o] = (unsigned)M | kSlotStart;
+            entries[o] = -1;
+            if (q >= S) continue;
+            const SlotCell& c = cell[(size_t)l * S + q];
+            unsigned w = c.flags | ((unsigned)c.pidx << kSlotPidxShift);
+            if (c.kind == 1) {
+                w |= (unsigned)col[row_ptr[c.row] + c.ent];
+                entries[o] = row_ptr[c.row] + c.ent;
+            } else if (c.kind == 2) {
+                w |= kSlotPart | (unsigned)c.part;
+                entries[o] = -2;
+            } else if (c.kind == 3) {
+                w |= kSlotClose | (unsigned)c.row;
+            } else {
+                w = (unsigned)M | kSlotStart;
+            }
+            words[o] = w;
+        }
+    *S_out = S;
+    *bar_out = SA;
+    *npart_out = np;
+    return SSS_OK;
 }
 
 int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg, const double* d_prog,

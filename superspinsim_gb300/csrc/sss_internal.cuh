@@ -22,6 +22,9 @@ constexpr int kCloseMax = 8;    // close slots per lane
 constexpr int kRing = 16;       // fine steps of coefficients per refill
 // (C parts per lane, P entries per part) shapes instantiated
 constexpr int kPartShapes[][2] = {{1, 4}, {2, 4}, {4, 4}, {2, 8}};
+// slot-packed kernels: slots per lane (S <= kSlotsMax)
+constexpr int kSlotsMax = 16;
+constexpr int kLaneCounts = 6;  // lanes per trajectory 8, 16, ..., 256 of the row kernels
 
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
@@ -72,6 +75,12 @@ struct BatchLayout {
     int C = 0, P = 0, kc = 0;
     std::vector<int> pcol;                   // C*P*L part entry columns [e][l]
     std::vector<unsigned> cw;                // kCloseMax*L close words [k][l]
+    // slot-packed and phased row-part variants: S FMA slots per lane per
+    // Horner term, kernel slot words in cw (load words [q][l], then store
+    // words [S+q][l]), a barrier before slot bar_at, npart parked partial
+    // sums per trajectory; phased: the shape index into kPhasedShapes
+    bool slots = false, phased = false;
+    int S = 0, bar_at = 0, npart = 0, shape = 0;
     std::vector<char> chan_const;            // per generator slot: its channel is batch-constant
     std::vector<double> chan_value;          // that constant
     std::vector<int> slot_chan;              // per generator slot: its program channel (-1: L0)
@@ -109,16 +118,18 @@ struct sss_plan {
     bool ev_recorded = false;
     bool ev_keep_begin = false;  // a later phase of one run: keep the first launch's begin event
     int auto_lanes_ntraj = 0;    // trajectories the automatic lane rule counts (0: the batch)
+    double auto_cost[sss::kLaneCounts] = {};  // last automatic layout: cost per lane count 8..256
     int launch_active = 0;       // trajectories with work in the next launch (0: the batch)
     // prepared batch (sss_batch_prepare -> sss_batch_launch): one kernel
     // layout per phase -- a single phase, or with uneven lengths and
     // automatic lanes one per widening lane count, phase k running from
     // output sample t_start on
     struct BatchPhase {
-        alignas(16) unsigned char args[1024];
+        alignas(16) unsigned char args[1536];
         size_t smem = 0;
-        int L = 0, C = 0, P = 0, epl = 0, threads = 0, t_start = 0;
-        bool use_reg = false, one_chain = false, parts = false, shfl = false;
+        int L = 0, C = 0, P = 0, epl = 0, threads = 0, t_start = 0, S = 0, shape = 0;
+        bool use_reg = false, one_chain = false, parts = false, shfl = false, slots = false,
+             phased = false;
     };
     BatchPhase batch_phase[sss::kMaxPhases];
     sss::DevBuf batch_tables[sss::kMaxPhases];
@@ -177,6 +188,8 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
                  bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts = false,
                  const double* d_tab = nullptr, int T_tab = 0);
+int slot_layout_host(int M, const int* row_ptr, const int* col, int L, int S_cap, int* S_out,
+                     int* bar_out, int* npart_out, unsigned* words, int* entries);
 int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows,
                       const std::vector<std::vector<char>>& prio, int L, int threads, int w_chain,
                       int w_close, const std::vector<int>& active,
@@ -184,7 +197,7 @@ int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::En
 // Row-part forward kernel prepared outside the plan's batch state (for the
 // adjoint): opaque kernel arguments and launch shape.
 struct PartsForward {
-    alignas(16) unsigned char args[1024];
+    alignas(16) unsigned char args[1536];
     size_t smem = 0;
     int L = 0, C = 0, P = 0, threads = 0;
 };

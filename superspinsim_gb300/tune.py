@@ -2,7 +2,8 @@
 
 Times short prepared launches of the actual batch (a few output samples of
 every trajectory) for each candidate configuration -- lanes per trajectory,
-kernel variant (two FMA chains per row, one, or row parts) and CTA size -- with CUDA
+kernel variant (two FMA chains per row, one, row parts, packed slots or
+phased row parts) and CTA size -- with CUDA
 events on the launch stream, keeps the fastest, and caches the choice per
 (model, batch size, fine steps) for the process.
 """
@@ -23,7 +24,8 @@ def _key(sweep, B, progs):
 
 
 def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, repeats=2,
-             lanes=(0, 8, 16, 32, 64, 128), variants=(1, 3, 4), threads=(32, 64, 128), use_cache=True):
+             lanes=(0, 8, 16, 32, 64, 128), variants=(1, 3, 4, 6, 7), threads=(32, 64, 128),
+             use_cache=True):
     """Pick and set the fastest batch configuration for this sweep and batch.
     Returns {"config": (lanes, variant, threads), "ms_per_traj_step": ...,
     "trials": [...]}."""

@@ -29,7 +29,9 @@ def _excited_weights(vmap):
 @pytest.mark.parametrize("name", ["nv7_n49", "nv7_n19"])
 @pytest.mark.parametrize("lanes,variant", [(0, 0), (1, 0), (4, 0), (32, 0), (0, 1), (16, 1),
                                            (0, 2), (8, 2), (0, 3), (32, 3), (0, 4), (8, 4),
-                                           (16, 4), (32, 4), (64, 4), (128, 4)])
+                                           (16, 4), (32, 4), (64, 4), (128, 4), (0, 6), (8, 6),
+                                           (16, 6), (32, 6), (64, 6), (128, 6), (0, 7), (8, 7),
+                                           (16, 7), (32, 7)])
 def test_batch_odmr_against_oracle(name, lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
@@ -58,7 +60,8 @@ def test_batch_odmr_against_oracle(name, lanes, variant):
     assert np.abs(ro - ref @ w).max() <= 1e-12
 
 
-@pytest.mark.parametrize("lanes,variant", [(0, 0), (0, 4), (64, 4)])
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (0, 4), (64, 4), (0, 6), (16, 6), (0, 7),
+                                           (32, 7)])
 def test_batch_uneven_lengths_and_plain_agree(lanes, variant):
     from superspinsim_gb300 import _lib
     from superspinsim_gb300.quadratures import method
@@ -106,7 +109,8 @@ def test_batch_empty_and_zero_state():
     assert ro.shape == (0, 3)
 
 
-@pytest.mark.parametrize("lanes,variant", [(0, 0), (16, 4), (32, 4)])
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (16, 4), (32, 4), (8, 6), (16, 6), (0, 6),
+                                           (8, 7), (16, 7), (32, 7)])
 def test_batch_ramsey_uneven_against_oracle(lanes, variant):
     """Uneven Ramsey protocol (laser init, pi/2 - tau - pi/2, laser readout)
     with per-trajectory lengths, against the oracle trajectory by trajectory."""
@@ -143,7 +147,8 @@ def test_batch_ramsey_uneven_against_oracle(lanes, variant):
         assert np.abs(fin[b] - ref[-1]).max() <= 1e-12
 
 
-@pytest.mark.parametrize("lanes,variant", [(0, 0), (32, 1), (128, 4), (256, 4)])
+@pytest.mark.parametrize("lanes,variant", [(0, 0), (32, 1), (128, 4), (256, 4), (128, 6),
+                                           (256, 6)])
 def test_batch_nv21_against_oracle(lanes, variant):
     """21-level NV with 14N (441 x 441), 4 ODMR trajectories: the register
     kernel and the row-part kernel with groups of 4 and 8 warps (one
@@ -179,7 +184,7 @@ def test_batch_nv21_against_oracle(lanes, variant):
     assert np.abs(fin - ref[:, -1]).max() <= 1e-12
 
 
-@pytest.mark.parametrize("variant", [0, 4])
+@pytest.mark.parametrize("variant", [0, 4, 6, 7])
 def test_chunked_runs_graph_replay_and_resume(tmp_path, variant):
     """Prepare once, launch in chunks: identical to the one-shot run; the
     chunk sequence captured in a CUDA graph replays to the same result; a
