@@ -1310,9 +1310,12 @@ bool slots_pack(const std::vector<int>& nent, int L, int S_cap, std::vector<Slot
 //     first part's partial sum, adds the other k - 1 partial sums (one slot
 //     each) and the r items left, (k - 1) + r <= P2.
 // Rows take the option with the fewest phase-1 chains; chains are dealt to
-// lanes round-robin.
-bool phased_pack(const std::vector<int>& nent, int L, const PhasedShape& sh, std::vector<SlotCell>& cell,
-                 int* npart_out) {
+// lanes round-robin.  items[i] lists row i's items in the order they are
+// dealt (entry indices, -1 for the v entry): the first n + 1 - r go to the
+// parts round-robin, so items early in the list sit at the lowest chain
+// positions of every part, and the last r to the phase-2 chain.
+bool phased_pack(const std::vector<int>& nent, const std::vector<std::vector<int>>& items, int L,
+                 const PhasedShape& sh, std::vector<SlotCell>& cell, int* npart_out) {
     const int M = (int)nent.size();
     const int C1 = sh.C1, P1 = sh.P1, C2 = sh.C2, P2 = sh.P2;
     const int S1 = C1 * P1, S = S1 + C2 * P2;
@@ -1344,12 +1347,12 @@ bool phased_pack(const std::vector<int>& nent, int L, const PhasedShape& sh, std
     }
     if (n1 > (long)C1 * L || n2 > (long)C2 * L) return false;
     auto at = [&](int l, int q) -> SlotCell& { return cell[(size_t)l * S + q]; };
-    // items of a row: its entries 0..n-1, then its v entry
     auto put_item = [&](SlotCell& c, int row, int it) {
+        const int e = items[row][it];
         c.row = row;
-        if (it < nent[row]) {
+        if (e >= 0) {
             c.kind = 1;
-            c.ent = it;
+            c.ent = e;
         } else {
             c.kind = 3;
         }
@@ -1359,14 +1362,17 @@ bool phased_pack(const std::vector<int>& nent, int L, const PhasedShape& sh, std
         const Choice& pl = plan[i];
         const int n = nent[i] + 1;
         const bool single = pl.k == 1 && pl.r == 0;
-        int it = 0;
+        const int in_parts = n - pl.r;
+        int it = in_parts;
         std::vector<int> parts;
         for (int k = 0; k < pl.k; k++) {
-            const int left = (n - pl.r) - it;
-            const int len = k == pl.k - 1 ? left : std::min(P1, left);
             const int lane = j1 % L, ch = j1 / L;
             j1++;
-            for (int e = 0; e < len; e++) put_item(at(lane, e * C1 + ch), i, it++);
+            // part k takes items k, k + pl.k, k + 2 pl.k, ... of the first in_parts
+            for (int e = 0, x = k; x < in_parts; e++, x += pl.k) {
+                if (e >= P1) return false;
+                put_item(at(lane, e * C1 + ch), i, x);
+            }
             SlotCell& last = at(lane, (P1 - 1) * C1 + ch);
             if (single) {
                 last.store_row = i;
@@ -1512,9 +1518,12 @@ int slots_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::En
 
 // Phased row-part layout at L lanes: the first shape of kPhasedShapes (in
 // order of slots per lane, at most S_cap) that fits.
+// varies[g] (per generator slot, may be empty): its coefficient varies, so
+// its entries are assembled every exponential.
 int phased_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows, int L,
                        int threads, int S_cap, const std::vector<int>& active,
-                       const std::vector<int>& rows_reached, BatchLayout* out) {
+                       const std::vector<int>& rows_reached, const std::vector<char>& varies,
+                       BatchLayout* out) {
     BatchLayout& Ly = *out;
     const int M = (int)rows.size();
     if (L != 8 && L != 16 && L != 32)
@@ -1523,12 +1532,29 @@ int phased_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::E
     if (M + 2 > (int)kSlotIdx) return fail(SSS_EINVAL, "phased row-part variant supports at most 16381 rows");
     std::vector<int> nent(M);
     for (int i = 0; i < M; i++) nent[i] = (int)rows[i].size();
+    // item order per row: entries of generators whose coefficient varies
+    // (assembled every exponential) first, then the others, then the v
+    // entry, so the varying entries of every chain sit at its first slots
+    // and the per-exponential assembly touches few slot positions
+    const SparseGenerators& sp = p->sparse;
+    std::vector<std::vector<int>> items(M);
+    for (int i = 0; i < M; i++) {
+        std::vector<int> later;
+        for (int e = 0; e < nent[i]; e++) {
+            bool var = false;
+            for (int g : active)
+                var |= g < (int)varies.size() && varies[g] && sp.val[(size_t)g * sp.nnz + rows[i][e].q] != 0.0;
+            (var ? items[i] : later).push_back(e);
+        }
+        items[i].insert(items[i].end(), later.begin(), later.end());
+        items[i].push_back(-1);
+    }
     std::vector<SlotCell> cell;
     int best = -1, npart = 0;
     for (int k = 0; k < kPhasedShapeCount && best < 0; k++) {
         const PhasedShape& sh = kPhasedShapes[k];
         if (sh.C1 * sh.P1 + sh.C2 * sh.P2 > S_cap) continue;
-        if (phased_pack(nent, L, sh, cell, &npart)) best = k;
+        if (phased_pack(nent, items, L, sh, cell, &npart)) best = k;
     }
     if (best < 0)
         return fail(SSS_EINVAL, "phased row-part variant does not fit this pattern at " +
@@ -1854,6 +1880,8 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
                                 "kernel (variant 0, 4, 6 or 7)");
     if (force_parts || (allow_register && (rot || table || row_kernels || p->batch_variant == 0))) {
         const int threads_cfg = p->batch_threads > 0 ? p->batch_threads : 32;
+        std::vector<char> varies(G, 0);
+        for (int g = 0; g < G; g++) varies[g] = Ly.slot_chan[g] >= 0 && !Ly.chan_const[g];
         // At Lc lanes: the cheapest of the row-part (0), phased row-part (1)
         // and slot-packed (2) layouts that fit (FP64 instructions per Horner
         // term, layout_cost); ties go to the earlier one (the phased
@@ -1872,7 +1900,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
             if (phased_ok && Lc <= 32 && cap[1] >= 1) {
                 BatchLayout tq;
                 if (phased_layout_rows(p, Ly.row_ents, Lc, threads_cfg, cap[1], active, rows_reached,
-                                       &tq) == SSS_OK)
+                                       varies, &tq) == SSS_OK)
                     cost[1] = layout_cost(tq);
             }
             double lim = 0.0;
@@ -1896,7 +1924,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
                                           rows_reached, out, nullptr);
                 else if (pick == 1)
                     r = phased_layout_rows(p, Ly.row_ents, Lc, threads_cfg, cap[1], active,
-                                           rows_reached, out);
+                                           rows_reached, varies, out);
                 else
                     r = slots_layout_rows(p, Ly.row_ents, Lc, threads_cfg, cap[2], active,
                                           rows_reached, out);
