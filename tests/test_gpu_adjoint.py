@@ -78,8 +78,9 @@ def test_adjoint_objective_matches_forward_and_fd(variant):
 
 
 def test_adjoint_matches_fd_of_oracle():
-    """Finite differences of the CPU oracle (the reference's integrator) on
-    one shape with two segments."""
+    """Finite differences of the CPU oracle in reference mode (the
+    reference's own algorithm: 4^-35 scaling and 70 residual squarings per
+    exponential) on one shape with two segments."""
     from superspinsim_gb300.adjoint import trapezoid_weights
     obj, c, rho = _objective()
     rabi, phase, progs, dur = _problem(seed=9, B=1, S=2, seg=1e-9, t_read=2e-9)
@@ -92,11 +93,11 @@ def test_adjoint_matches_fd_of_oracle():
 
     def J_oracle(p):
         _, d = oracle.simulate(c["generators"], rho, 0.0, T*dt + 1e-13, dt, p, K=2, W=W,
-                               nodes=nodes, F=100, vectorisation_map=vm, mode="vector",
-                               degree=16, flat_out=True)
+                               nodes=nodes, F=100, vectorisation_map=vm, mode="reference",
+                               flat_out=True)
         return float((d @ obj.rw) @ tw)
 
-    assert abs(J_oracle(progs[0]) - J[0]) <= 1e-12*abs(J[0])
+    assert abs(J_oracle(progs[0]) - J[0]) <= 1e-11*abs(J[0])
     for s in range(2):
         for comp, col, h in ((0, 2, 1e-6*progs[0, 0, s, 2]), (1, 4, 1e-6)):
             pp, pm = progs[0].copy(), progs[0].copy()
