@@ -47,9 +47,6 @@ F_RES = 2.870e9 + GAMMA*B_FIELD
 RABI = 5e6
 LASER = 10/65.9
 METRIC = "NV-7 ODMR traj-steps/s"
-# DRAM bytes (read + write) of one batched-kernel launch on this workload,
-# from ncu (profiles/batch_odmr_nv7.md)
-TRAFFIC_BYTES = 880896
 
 
 def nv7_model():
@@ -199,16 +196,77 @@ def max_over_ranks(x, world):
     return replicas.max_over_ranks(x) if world > 1 else x
 
 
-def flops_per_traj_step(info, G, K):
-    """Executed FP64 flops of one trajectory step of the batched kernel:
-    per exponential and sub-step, assembly of Omega on the pruned pattern
-    (2 G nnz) and d Taylor terms (2 nnz multiply-adds + 2 rows for the
-    scaling and accumulation)."""
+def executed_flops_per_traj_step(info, K):
+    """FP64 flops one trajectory step of the batched kernel computes: per
+    exponential, the assembly of the generators whose coefficient varies on
+    their non-zeros of the pruned pattern (2 live_nnz; the constant ones are
+    a precomputed table), and per sub-step d Taylor terms of 2 flops per
+    non-zero and 2 per row (its v term) plus one multiply per row (the
+    scaled form's 1/d!)."""
     nnz, rows, d, m = info["nnz"], info["rows"], info["degree"], info["substeps"]
-    return K*(2*G*nnz + m*d*(2*nnz + 2*rows))
+    return K*(2*info["live_nnz"] + m*(d*(2*nnz + 2*rows) + rows))
+
+
+def dense_flops_per_traj_step(N, G, K, m):
+    """The dense formula K (2 G N^2 + m 2 N^3 + 2 N^2) with m matrix products
+    per exponential, for comparison (the reference's scheme has m = 70)."""
+    return K*(2*G*N*N + m*2*N**3 + 2*N*N)
+
+
+def fp64_issue_per_traj_step(info, K, L):
+    """FP64 warp instructions one trajectory step issues (its share of its
+    group's instructions): d terms of fp64_per_term instructions per
+    exponential and sub-step, over the 32/L trajectories of a warp."""
+    per_group = K*info["substeps"]*info["degree"]*info["fp64_per_term"]
+    return per_group*min(L, 32)/32
 
 
 CPU_SAMPLES = 16   # output samples of the bounded CPU sample (x F fine steps)
+
+
+def full_length_parity(plan, N):
+    """The workload's trajectory nearest the ms=0 -> +1 line over all
+    400,000 steps through the batched kernel (the layout the bench chose),
+    against the reference's own algorithm: the fixture of the oracle's
+    reference mode (70 squarings per exponential), tests/golden/
+    nv7_fullrun.npz.  Density max-abs at every 100th sample and the
+    fluorescence at every sample."""
+    path = os.path.join(ROOT, "tests", "golden", "nv7_fullrun.npz")
+    with np.load(path) as z:
+        fx = {k: z[k] for k in z.files}
+    T, dt, Fx = int(fx["T"]), float(fx["dt"]), int(fx["F"])
+    ro, _, tr = plan.batch(fx["rho0"][None], fx["program"][None], 0.0, dt, T, Fx,
+                           readout_weights=fx["readout_weights"], want_trace=True)
+    ref_f = fx["fluorescence"]
+    return {"vs": "the reference's algorithm (oracle reference mode, 70 squarings per "
+                  "exponential) on the sweep's trajectory nearest resonance, all 400,000 "
+                  "steps (tests/golden/nv7_fullrun.npz)",
+            "density_max_abs": float(np.abs(tr[0][fx["kept_samples"]] - fx["states"]).max()),
+            "fluorescence_rel_max": float(np.abs(ro[0] - ref_f).max()/np.abs(ref_f).max()),
+            "bars": {"density_max_abs": 1e-10, "fluorescence_rel": 1e-9}}
+
+
+def cpu_vector_baseline(threads=0, n_freq=N_FREQ, n_traj=64, T_s=64):
+    """The batched kernel's own algorithm on the host cores (the CPU
+    oracle's vector mode: the sparse Taylor action, degree 16) on a bounded
+    sample of the workload: its first n_traj trajectories for T_s output
+    samples of F = 200 steps, trajectories spread over the cores."""
+    from oracle import oracle
+    from superspinsim_gb300.quadratures import method
+    gens, vm = nv7_model()
+    progs, rho = workload(n_freq)
+    W, nodes = method(K_EXP)
+    t = time.perf_counter()
+    oracle.simulate(gens, np.stack([rho]*n_traj), 0.0, T_s*DT_OUT + DT_OUT*1e-4, DT_OUT,
+                    progs[:n_traj], K=K_EXP, W=W, nodes=nodes, F=F, vectorisation_map=vm,
+                    mode="vector", degree=16, threads=threads, flat_out=True)
+    el = time.perf_counter() - t
+    n = n_traj*T_s*F
+    return {"value": n/el, "unit": "traj-steps/s", "cores": threads or oracle.max_threads(),
+            "kind": "port",
+            "sample": f"trajectories 0-{n_traj - 1} of the workload, {T_s} samples x F={F} "
+                      f"each ({n} CF4:2 steps), the batched kernel's algorithm (sparse Taylor "
+                      f"action on the reachable pattern)"}
 
 
 def cpu_baseline(steps=None, threads=0, n_freq=N_FREQ):
@@ -305,6 +363,56 @@ def adjoint_workload(nv21=False, n_traj=0):
     return obj, progs, T, tw, S, "NV-21" if nv21 else "NV-7"
 
 
+def adjoint_measurement(steps=2, warmup=1):
+    """The adjoint half of the metric on its workload (NV-7, 256 pulse shapes
+    x 128 segments, 256 parameters each): gradients/s, the ratio to one
+    forward solve, and four gradient entries of one shape against central
+    differences of the GPU forward with h = 1e-6 (relative for amplitudes),
+    with the clocks sampled while it runs."""
+    import torch
+    obj, progs, T, tw, S, name = adjoint_workload(False)
+    B = progs.shape[0]
+    for _ in range(warmup):
+        obj.run(progs, DT_OUT, T, tw)
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    fwd, adj = [], []
+    for _ in range(steps):
+        t = time.perf_counter()
+        obj.forward_only(progs, DT_OUT, T, tw)
+        fwd.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        J, grad = obj.run(progs, DT_OUT, T, tw)
+        adj.append(time.perf_counter() - t)
+    clock_info = clocks.stop()
+    fwd_s, adj_s = statistics.median(fwd), statistics.median(adj)
+    b = 1
+    pert, idx = [], []
+    for seg in (0, S//2):
+        for comp, col in ((0, 2), (1, 4)):
+            h = 1e-6*progs[b, 0, seg, 2] if comp == 0 else 1e-6
+            for step in (h, -h):
+                pp = progs[b].copy()
+                pp[0, seg, col] += step
+                pert.append(pp)
+            idx.append((seg, comp, h))
+    Jp = obj.forward_only(np.stack(pert), DT_OUT, T, tw)
+    errs = []
+    for k, (seg, comp, h) in enumerate(idx):
+        fd = (Jp[2*k] - Jp[2*k + 1])/(2*h)
+        errs.append(abs(grad[b, seg, comp] - fd)/max(abs(fd), 1e-300))
+    return {"value": B/adj_s, "unit": f"gradients/s ({2*S} parameters each)",
+            "workload": f"{name}, {B} pulse shapes x {S} segments of 2 ns + 300 ns laser "
+                        f"readout, dt 5 ps ({T*F:,} steps each); objective: integrated "
+                        f"fluorescence over the readout",
+            "ms_per_gradient_batch": 1e3*adj_s, "adjoint_over_forward": adj_s/fwd_s,
+            "forward_traj_steps_per_s": B*T*F/fwd_s,
+            "fd_check": {"shape": b, "entries": len(errs), "h": 1e-6,
+                         "rel_err_max": float(max(errs))},
+            "clocks": clock_info}
+
+
 def run_adjoint_workload(args, rank, world):
     """Times the checkpointed adjoint (objective + 2S gradients per shape)
     of adjoint_workload against one forward solve of the same batch."""
@@ -357,6 +465,8 @@ def main():
     ap.add_argument("--graph-chunk", type=int, default=0,
                     help="time a CUDA graph of the prepared run in chunks of this many output "
                          "samples (resumable launches) instead of one launch")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the adjoint measurement of the default line")
     ap.add_argument("--rotating", action="store_true",
                     help="run the batch in the generalised rotating frame (simspins' default)")
     args = ap.parse_args()
@@ -374,10 +484,17 @@ def main():
     from superspinsim_gb300.sweep import Sweep, population_weights, trapezoid
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    gens, vm, progs, rho, samples, T, levels, wdesc = build_workload(args.workload, args)
+    gens, vm, progs_all, rho, samples_all, T, levels, wdesc = build_workload(args.workload, args)
     N = vm.shape[0]
+    B_all = progs_all.shape[0]
+    # the sweep's trajectories are sharded over the ranks (contiguous ranges,
+    # no device collective); the job's units are the whole sweep's
+    from superspinsim_gb300 import replicas
+    t_begin, t_end = replicas.shard(B_all, rank, world)
+    progs = progs_all[t_begin:t_end]
+    samples = None if samples_all is None else samples_all[t_begin:t_end]
     B = progs.shape[0]
-    units_per_step = int(samples.sum())*F if samples is not None else B*T*F
+    units_per_step = int(samples_all.sum())*F if samples_all is not None else B_all*T*F
     rho0 = np.repeat(flatten_density(rho, N, vm)[None], B, axis=0)
     w = population_weights(vm, levels)
     sweep = Sweep(gens, vm, number_of_exponentials=K_EXP, number_of_fine_divisions=F,
@@ -443,7 +560,7 @@ def main():
     info = plan.batch_info()
     launches = (n_chunks or plan.last_launches())*args.steps
     total_ms = max_over_ranks(sum(times), world)
-    units = units_per_step*world*args.steps
+    units = units_per_step*args.steps
     value = units/(total_ms/1e3)
 
     # e2e: public API, host buffers in and out, every step
@@ -452,14 +569,14 @@ def main():
         torch.cuda.synchronize()
         barrier(world)
         t = time.perf_counter()
-        out = sweep.run(np.repeat(rho[None], B, axis=0), progs, 0.0, T*DT_OUT + 1e-13,
-                        DT_OUT, samples=samples, readout_weights=w)
+        out = sweep.run_sharded(np.repeat(rho[None], B_all, axis=0), progs_all, 0.0,
+                                T*DT_OUT + 1e-13, DT_OUT, samples=samples_all, readout_weights=w)
         fluor = 65.9e6*trapezoid(out["readout"], DT_OUT)
         el = time.perf_counter() - t
         if i >= 1:
             e2e_times.append(el)
     e2e_s = max_over_ranks(sum(e2e_times), world)
-    e2e_value = units_per_step*world*args.steps/e2e_s
+    e2e_value = units_per_step*args.steps/e2e_s
     h2d = rho0.nbytes + progs.nbytes + (samples.nbytes if samples is not None else 0)
     d2h = B*T*8
 
@@ -470,7 +587,7 @@ def main():
     if N <= 52:
         plain_sim = generate_simulator(progs[0], gens, vm, number_of_exponentials=K_EXP,
                                        number_of_fine_divisions=F)
-        plain_T = 64
+        plain_T = T  # one whole trajectory: T step-propagator CTAs fill the GPU
         plain_sim(rho, 0.0, 8*DT_OUT + 1e-13, DT_OUT)
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -478,16 +595,24 @@ def main():
         plain_s = time.perf_counter() - t
         plain_value = plain_T*F/plain_s
 
-    fl = flops_per_traj_step(info, gens.shape[0], K_EXP)
+    fl = executed_flops_per_traj_step(info, K_EXP)
+    issue = fp64_issue_per_traj_step(info, K_EXP, info["lanes"])
     # the kernel's device time per step: the launch's own events, or with
     # graph chunks (events of the last chunk only) the step's event time
     kms = statistics.mean(kernel_ms) if not n_chunks else statistics.mean(times)
-    achieved = fl*units_per_step/(kms*1e-3)/1e12
+    local_units = (int(samples.sum())*F if samples is not None else B*T*F)
+    achieved = fl*local_units/(kms*1e-3)/1e12
     peak = _lib.fp64_peak_tflops()
     mma_peak = _lib.fp64_mma_peak_tflops()
+    # FP64 warp-instruction slots of the GPU per second at the peak rate
+    # (the peak's FMAs per second over 32 lanes)
+    issue_peak = peak*1e12/2/32
+    # algorithmic DRAM bytes of one launch: initial states and programs read
+    # once, readouts written once
+    traffic = rho0.nbytes + progs.nbytes + B*T*8 + (samples.nbytes if samples is not None else 0)
     line = {"metric": METRIC, "value": value, "unit": "traj-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms/args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {**wdesc, "method": "CF4:2",
                        "dt_s": DT_OUT/F, "samples": T, "fine_divisions": F,
@@ -499,11 +624,14 @@ def main():
                            "trials": len(tuned["trials"])},
                        "kernel": {"lanes": info["lanes"], "taylor_degree": info["degree"],
                                   "substeps": info["substeps"], "rows": info["rows"],
-                                  "nnz": info["nnz"],
+                                  "nnz": info["nnz"], "variant": info["variant"],
+                                  "live_generators": info["live_generators"],
+                                  "live_nnz": info["live_nnz"],
+                                  "fp64_per_horner_term": info["fp64_per_term"],
                                   # uneven lengths run in phases of widening lane
                                   # groups; "lanes" is the last phase's
                                   "launches_per_run": n_chunks or plan.last_launches()},
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"trajectory shards x{world}"},
             "e2e": {"value": e2e_value, "unit": "traj-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
@@ -514,11 +642,26 @@ def main():
                 "batched_over_plain": value/plain_value},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved/peak,
-                         "traffic": TRAFFIC_BYTES if args.workload == "odmr" else None,
-                         "traffic_note": "dram read+write of one launch from an ncu capture "
-                                         "(profiles/batch_odmr_nv7.md); inputs are read once, "
-                                         "so it does not grow with the step count",
+                         "traffic": traffic,
+                         "traffic_note": "bytes of one launch: initial states and programs "
+                                         "read once, readouts written once (the kernel keeps "
+                                         "its working set in shared memory; an ncu capture of "
+                                         "the same kernel at 20 samples read 630 B of DRAM, "
+                                         "its 0.16 MB of readouts staying in L2)",
                          "peak_source": "measured live (sss_fp64_peak DFMA loop)",
+                         "flops_note": "executed: assembly of the drive generators on their "
+                                       "non-zeros, d Taylor terms of 2 flops per non-zero "
+                                       "and per row, 1/d! per row",
+                         "fp64_issue": {"per_traj_step": issue,
+                                        "achieved_per_s": issue*local_units/(kms*1e-3),
+                                        "peak_per_s": issue_peak,
+                                        "frac": issue*local_units/(kms*1e-3)/issue_peak,
+                                        "note": "FP64 warp instructions issued (lanes of a "
+                                                "warp instruction not carrying a flop count "
+                                                "here but not in `achieved`)"},
+                         "dense_formula_flops_per_traj_step": {
+                             "m_70": dense_flops_per_traj_step(N, gens.shape[0], K_EXP, 70),
+                             "note": "the reference's scheme, K (2 G N^2 + 70 x 2 N^3 + 2 N^2)"},
                          "fp64_tensor": {"dmma_peak": mma_peak, "unit": "TFLOP/s",
                                          "used": False,
                                          "note": "measured live (sss_fp64_mma_peak, mma.sync "
@@ -530,23 +673,29 @@ def main():
     if args.workload != "odmr":
         line["metric"] = {"ramsey": "NV-7 Ramsey (uneven) traj-steps/s",
                           "nv21": "NV-21 ODMR traj-steps/s"}[args.workload]
+    if rank == 0 and world == 1 and args.workload == "odmr" and not args.rotating and \
+            args.n_freq == N_FREQ and args.duration == DURATION:
+        line["parity"] = full_length_parity(plan, N)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "odmr" \
             and not args.rotating:
         cb = cpu_baseline(n_freq=args.n_freq)
         cb.pop("seconds", None)
         ref = cb.pop("states")
         line["cpu_baseline"] = cb
-        # parity: the same trajectory and window through the batched path,
-        # against the reference algorithm's states
+        line["cpu_algorithm_matched"] = cpu_vector_baseline(n_freq=args.n_freq)
+        # the same trajectory and window through the batched path, against
+        # the reference algorithm's states of the CPU baseline run
         ro_p, _, tr_p = plan.batch(rho0[:1], progs[:1], 0.0, DT_OUT, CPU_SAMPLES, F,
                                    readout_weights=w, want_trace=True)
         fl_ref = ref @ w
-        line["parity"] = {
-            "vs": "the reference's algorithm (CPU oracle, reference mode) on trajectory 0, "
-                  f"{CPU_SAMPLES} samples x F={F}",
+        line["parity_cpu_window"] = {
+            "vs": "the reference's algorithm (CPU oracle, reference mode) run live on "
+                  f"trajectory 0, {CPU_SAMPLES} samples x F={F}",
             "density_max_abs": float(np.abs(tr_p[0] - ref).max()),
-            "fluorescence_rel_max": float(np.abs(ro_p[0] - fl_ref).max()/np.abs(fl_ref).max()),
-            "bars": {"density_max_abs": 1e-10, "fluorescence_rel": 1e-9}}
+            "fluorescence_rel_max": float(np.abs(ro_p[0] - fl_ref).max()/np.abs(fl_ref).max())}
+    if rank == 0 and world == 1 and args.workload == "odmr" and not args.rotating and \
+            not args.no_adjoint:
+        line["adjoint"] = adjoint_measurement()
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -320,6 +320,15 @@ int sss_slot_layout(int M, const int* row_ptr, const int* col, int lanes,
                     int max_slots, int* slots, int* barrier_slot, int* partials,
                     unsigned* words, int* entries);
 
+/* What the last batched run executes (no reference counterpart; for the
+ * roofline count): the kernel variant chosen (1-7, as
+ * sss_plan_set_batch_config), the generators assembled per exponential
+ * (those whose coefficient varies; the constant ones are folded into a
+ * table), their non-zeros on the pruned pattern, and the FP64 instructions
+ * one group issues per Horner term.  Any pointer may be NULL. */
+int sss_plan_batch_work(const sss_plan* plan, int* variant, int* live_generators,
+                        int* live_nnz, int* fp64_per_term);
+
 /* Measurement utility (no reference counterpart): FP64 FMA throughput of
  * the current device in TFLOP/s, from a bounded DFMA loop (8 independent
  * chains per thread, 4 CTAs of 256 threads per SM).  The roofline

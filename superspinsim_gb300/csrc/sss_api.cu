@@ -586,6 +586,16 @@ int sss_plan_set_adjoint_memory(sss_plan* p, size_t max_bytes) {
     return SSS_OK;
 }
 
+int sss_plan_batch_work(const sss_plan* p, int* variant, int* live_generators, int* live_nnz,
+                        int* fp64_per_term) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (variant) *variant = p->last_variant;
+    if (live_generators) *live_generators = p->last_n_live;
+    if (live_nnz) *live_nnz = p->last_live_nnz;
+    if (fp64_per_term) *fp64_per_term = p->last_fp64_per_term;
+    return SSS_OK;
+}
+
 int sss_plan_batch_info(const sss_plan* p, int* lanes, int* degree, int* substeps, int* rows,
                         int* nnz, double* kernel_ms) {
     if (!p) return fail(SSS_EINVAL, "null plan");

@@ -2208,6 +2208,18 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
         a.n_lch = (int)lch.size();
         for (size_t i = 0; i < lch.size(); i++) a.lch_chan[i] = lch[i];
     }
+    // pattern entries with a non-zero value in some live generator
+    {
+        int lnnz = 0;
+        for (const auto& re : Ly.row_ents)
+            for (const BatchLayout::Ent& en : re) {
+                bool nz = false;
+                for (int gi : live) nz |= p->sparse.val[(size_t)active[gi] * p->sparse.nnz + en.q] != 0.0;
+                lnnz += nz;
+            }
+        p->mk_n_live = (int)live.size();
+        p->mk_live_nnz = lnnz;
+    }
     if (Ly.slots) {
         a.S = Ly.S;
         a.bar_at = Ly.bar_at;
@@ -2388,6 +2400,9 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
             p->last_epl = Ly.E;
             p->last_active = Ly.Ga;
             p->last_variant = Ly.phased ? 7 : Ly.slots ? 6 : Ly.parts ? 4 : Ly.use_reg ? (ph.one_chain ? 3 : 1) : 2;
+            p->last_n_live = p->mk_n_live;
+            p->last_live_nnz = p->mk_live_nnz;
+            p->last_fp64_per_term = Ly.slots ? Ly.S : Ly.parts ? Ly.C * Ly.P + Ly.kc : Ly.E;
         }
         if (!phased || !Ly.parts) break;
         // the next phase starts at the first sample where the automatic

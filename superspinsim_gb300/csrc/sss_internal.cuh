@@ -110,6 +110,10 @@ struct sss_plan {
     int batch_threads = 0;  // CTA size of the batched kernel, 0: 128
     int last_batch_lanes = 0, last_degree = 0, last_substeps = 0, last_rows = 0,
         last_nnz = 0, last_grid = 0, last_epl = 0, last_active = 0, last_variant = 0;
+    // executed work of the last prepared batch (phase 0): generators assembled
+    // per exponential, their non-zeros on the pruned pattern, FP64
+    // instructions per Horner term per group; make_args records the first two
+    int last_n_live = 0, last_live_nnz = 0, last_fp64_per_term = 0, mk_n_live = 0, mk_live_nnz = 0;
     int batch_variant = 0;  // 0: register variant when it fits, 2: shared-memory variant,
                             // 3: one-chain register variant, 4: row-part variant
     int device = 0;

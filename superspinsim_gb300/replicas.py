@@ -71,3 +71,27 @@ def gather_rows(local, n_total):
     out = np.concatenate(parts, axis=0)
     assert out.shape[0] == n_total
     return out
+
+
+def run_sharded(runner, n_total, gather=True):
+    """Run this rank's contiguous share [begin, end) of n_total trajectories
+    through runner(begin, end), which returns a dict of arrays whose leading
+    dimension is its trajectories (other values pass through unchanged),
+    and, with gather, assemble every such array over the ranks in
+    trajectory order.  Single process: runner(0, n_total)."""
+    rank, size = world()
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        rank, size = 0, 1
+    begin, end = shard(n_total, rank, size)
+    out = runner(begin, end)
+    if not gather or size == 1:
+        return out
+    res = {}
+    for k, v in out.items():
+        if isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == end - begin and \
+                k not in ("time",):
+            res[k] = gather_rows(v, n_total)
+        else:
+            res[k] = v
+    return res

@@ -89,6 +89,38 @@ class Sweep:
             return np.ascontiguousarray(rho0, dtype=np.float64)
         return flatten_density(rho0, self.N, self.vectorisation_map)
 
+    def run_sharded(self, rho0, programs, time_start, time_end, time_step, samples=None,
+                    readout_weights=None, final_state=False, gather=True):
+        """run() over the ranks of a multi-process job (one process per GPU,
+        torchrun environment): each rank runs its contiguous range of the
+        trajectories and, with gather, every rank receives the full
+        readouts and final states in trajectory order.  No device
+        collective; the host gather is the only exchange."""
+        from superspinsim_gb300 import replicas
+        if isinstance(programs, (list, tuple)):
+            progs = list(programs)
+        else:
+            progs = np.ascontiguousarray(programs, dtype=np.float64)
+        B = len(progs)
+        flat = self.flatten(rho0)
+        if flat.shape[0] == 1 and B > 1:
+            flat = np.repeat(flat, B, axis=0)
+
+        def runner(b, e):
+            if e <= b:
+                T = number_of_samples(time_start, time_end, time_step)
+                out = {"time": time_start + time_step*(np.arange(T) + 1)}
+                if readout_weights is not None:
+                    out["readout"] = np.zeros((0, T))
+                if final_state:
+                    out["final"] = np.zeros((0, flat.shape[1]))
+                return out
+            return self.run(flat[b:e], progs[b:e], time_start, time_end, time_step,
+                            samples=None if samples is None else np.asarray(samples)[b:e],
+                            readout_weights=readout_weights, final_state=final_state)
+
+        return replicas.run_sharded(runner, B, gather=gather)
+
     def run(self, rho0, programs, time_start, time_end, time_step, samples=None,
             readout_weights=None, final_state=False):
         """rho0: (B, n, n) complex or (B, N) flattened; programs: list of

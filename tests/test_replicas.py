@@ -51,3 +51,60 @@ def test_two_rank_gloo_gather_and_max():
         full, mx = out[rank]
         assert full == want
         assert mx == 11.0
+
+
+def _sharded_worker(rank, size, port, out):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(size), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    replicas.init(backend="gloo")
+    progs, rho, kw = _spin1_sweep()
+    from oracle import oracle
+
+    def runner(b, e):
+        # this rank's trajectories through the CPU oracle (the stand-in for
+        # the batched GPU run on a CPU-only test)
+        if e <= b:
+            return {"states": np.zeros((0,) + kw["shape"])}
+        _, st = oracle.simulate(kw["gens"], np.stack([rho]*(e - b)), 0.0, kw["tf"], kw["dt"],
+                                progs[b:e], K=2, W=kw["W"], nodes=kw["nodes"], F=kw["F"],
+                                vectorisation_map=kw["vm"], mode="vector", flat_out=True)
+        return {"states": st, "rank_of_row": np.full(e - b, rank)}
+
+    res = replicas.run_sharded(runner, progs.shape[0])
+    out[rank] = (res["states"].tolist(), res["rank_of_row"].tolist())
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+def _spin1_sweep():
+    """Seven spin-1 ODMR trajectories (the C1 model), 3 samples of 1 ns, F = 10."""
+    from conftest import load_case, quadrature
+    c = load_case("spin1_c1")
+    W, nodes = quadrature(2)
+    progs = np.repeat(c["program"][None], 7, axis=0)
+    progs[:, 0, 0, 3] = 2.870e9 + 28.025e9*0.01 + np.linspace(-20e6, 20e6, 7)
+    kw = {"gens": c["generators"], "vm": c["vectorisation_map"], "W": W, "nodes": nodes,
+          "F": 10, "dt": 1e-9, "tf": 3e-9 + 1e-13, "shape": (3, c["generators"].shape[1])}
+    return progs, c["rho0"], kw
+
+
+def test_two_rank_sharded_sweep_equals_single_process():
+    """Each of two gloo ranks runs its contiguous share of a sweep (3 and 4
+    of 7 trajectories); the gathered states equal the single-process run and
+    keep trajectory order."""
+    from oracle import oracle
+    with socket.socket() as sck:
+        sck.bind(("127.0.0.1", 0))
+        port = sck.getsockname()[1]
+    mgr = mp.get_context("spawn").Manager()
+    out = mgr.dict()
+    mp.start_processes(_sharded_worker, args=(2, port, out), nprocs=2, join=True,
+                       start_method="spawn")
+    progs, rho, kw = _spin1_sweep()
+    _, want = oracle.simulate(kw["gens"], np.stack([rho]*7), 0.0, kw["tf"], kw["dt"], progs, K=2,
+                              W=kw["W"], nodes=kw["nodes"], F=kw["F"],
+                              vectorisation_map=kw["vm"], mode="vector", flat_out=True)
+    for rank in range(2):
+        states, owner = out[rank]
+        assert np.array_equal(np.array(states), want)
+        assert owner == [0]*4 + [1]*3
