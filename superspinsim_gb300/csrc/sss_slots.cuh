@@ -8,7 +8,8 @@
 //     u_{j-1} = c_j v + Omega u_j,   c_j = d!/(j-1)!,   e^Omega v ~ u_0 / d!
 // (u_j = (d!/j!) w_j for the usual Horner iterates w_{j-1} = v + Omega w_j/j),
 // so the v term of a row is one more FMA entry with the uniform coefficient
-// c_j and a row of n entries costs n + 1 slots.  The host lays the pieces
+// c_j and a row of n entries costs n + 1 slots.  The last term drops the v
+// term: e^Omega v ~ v + (Omega u_1)/d!.  The host lays the pieces
 // of rows out lane by lane (slots_layout_rows, phased_layout_rows in
 // sss_batch.cu); per slot a lane loads its operand (an entry of the current
 // iterate, of v, or a parked partial sum) and computes
@@ -344,17 +345,21 @@ __global__ void __launch_bounds__(256, 1) k_batch_slots(const BatchArgs a) {
             }
             for (int m = 0; m < a.substeps; m++) {
                 // Horner terms j = d .. 1: V -> A, then A -> B, B -> A, ...
+                // The last term (j = 1) leaves the v term out and computes
+                // Omega u_1 alone; the row becomes v + (Omega u_1)/d!, so the
+                // rounded 1/d! scales only that small correction and no
+                // bias builds up in the state over many exponentials.
                 const int d = a.degree;
-                program.template term<0>(om, a.cfac[d], 0, lds, sts, gsync);
+                program.template term<0>(om, d == 1 ? 0.0 : a.cfac[d], 0, lds, sts, gsync);
                 int j = d - 1;
                 for (; j >= 2; j -= 2) {
                     program.template term<1>(om, a.cfac[j], MsB, lds, sts, gsync);
-                    program.template term<2>(om, a.cfac[j - 1], 0, lds, sts, gsync);
+                    program.template term<2>(om, j == 2 ? 0.0 : a.cfac[j - 1], 0, lds, sts, gsync);
                 }
-                if (j == 1) program.template term<1>(om, a.cfac[1], MsB, lds, sts, gsync);
-                // u_0 (in A for odd d, B for even d) / d! becomes v
+                if (j == 1) program.template term<1>(om, 0.0, MsB, lds, sts, gsync);
+                // Omega u_1 is in A for odd d, B for even d
                 const double* res = (d & 1) ? A : B;
-                for (int row = r0; row < r1; row++) V[row] = res[row] * a.inv_dfact;
+                for (int row = r0; row < r1; row++) V[row] = fma(res[row], a.inv_dfact, V[row]);
                 gsync();
             }
         }

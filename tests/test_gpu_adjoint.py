@@ -43,7 +43,10 @@ def test_adjoint_objective_matches_forward_and_fd(variant):
     tw = trapezoid_weights(T, dt, int(round(S*2e-9/dt)) - 1, T - 1)
     J, grad = obj.run(progs, dt, T, tw)
     Jf = obj.forward_only(progs, dt, T, tw)
-    assert np.abs(J - Jf).max() <= 1e-13*np.abs(Jf).max()
+    # the adjoint's forward pass and forward_only may run different kernel
+    # layouts (row parts with the usual Horner iterates, or the scaled
+    # Horner of the phased and slot-packed kernels): equal to rounding
+    assert np.abs(J - Jf).max() <= 1e-12*np.abs(Jf).max()
     # central differences of the GPU forward, all parameters in one batch,
     # Richardson-extrapolated from steps h and 2h (h = 1e-3): truncation
     # O(h^4) ~ 1e-12 and J's accumulated roundoff (~1e-14 relative) costs
@@ -176,7 +179,10 @@ def test_adjoint_nv21_wide_groups_match_fd():
     assert obj.plan.last_launches() == 2     # row-part forward + backward, no fallback
     assert obj.plan.batch_info()["lanes"] > 32
     Jf = obj.forward_only(progs, dt, T, tw)
-    assert np.abs(J - Jf).max() <= 1e-13*np.abs(Jf).max()
+    # the adjoint's forward pass and forward_only may run different kernel
+    # layouts (row parts with the usual Horner iterates, or the scaled
+    # Horner of the phased and slot-packed kernels): equal to rounding
+    assert np.abs(J - Jf).max() <= 1e-12*np.abs(Jf).max()
     pert, idx = [], []
     for b in range(B):
         for s in range(S):

@@ -178,7 +178,10 @@ def test_adjoint_full_size_against_fd(nv21):
     # S pulse segments and the readout segment of channel 0
     assert grad.shape == (B, S + 1, 2) and np.all(np.isfinite(grad)) and np.all(J > 0)
     Jf = obj.forward_only(progs, dt, T, tw)
-    assert np.abs(J - Jf).max() <= 1e-13*np.abs(Jf).max()
+    # the adjoint's forward pass and forward_only may run different kernel
+    # layouts (row parts with the usual Horner iterates, or the scaled
+    # Horner of the phased and slot-packed kernels): equal to rounding
+    assert np.abs(J - Jf).max() <= 1e-12*np.abs(Jf).max()
     b = 1
     pert, idx = [], []
     for s in (0, S//2, S - 1):
