@@ -28,10 +28,13 @@ Physical models supported: electron spin with zero-field splitting, g
 tensor (isotropic/axial), bias field, Lindblad dephasing (TS2) and
 Boltzmann thermalisation (TS1); nucleus with quadrupole, nuclear g,
 dephasing and thermalisation; hyperfine coupling; spin-spin (J) coupling
-within a block; and the NV inter-block couplings (spin-conserving and
-non-conserving optical excitation/decay, intersystem crossing both ways).
-Coherent block couplings ("coh") and the hBN Bell-state couplings raise
-NotImplementedError.
+within a block; the NV inter-block couplings (spin-conserving and
+non-conserving optical excitation/decay, intersystem crossing both ways);
+the hBN-style Bell-state couplings between a singlet and a pair of
+spin-1/2 atoms; and coherent (Hamiltonian) couplings between blocks,
+constant or scaled by the fourth control channel, whose blocks' mutual
+coherences join the allowed set through the transitive closure of the
+coupling graph.
 """
 import copy
 import math
@@ -400,14 +403,88 @@ def _incoherent(initial, final, dim):
     return [np.outer(vf, vi).astype(complex)]
 
 
-def _block_coupling(a, b, inter, dim, label_prefix):
-    """Jumps of one group interaction; returns {label: operator}."""
+def _coherent(initial, final, dim):
+    """Hermitian couplings between the states of `initial` and those of
+    `final` (reference _couple_coherent, generate_generators.py:2026-2058):
+    pairwise when the counts match, else one operator coupling every
+    initial state to every final state.  The reference builds the second
+    form with a bitwise or on float arrays, which raises a TypeError, so
+    that branch follows its evident intent and no fixture pins it."""
+    si, sf = _states_of(initial), _states_of(final)
+    if len(si) == len(sf):
+        out = []
+        for i, f in zip(si, sf):
+            H = np.zeros((dim, dim), complex)
+            H[f, i] = 1
+            H[i, f] = 1
+            out.append(H)
+        return out
+    vi = (np.abs(initial).sum(axis=0) > 0).astype(float)
+    vf = (np.abs(final).sum(axis=0) > 0).astype(float)
+    return [np.maximum(np.outer(vf, vi), np.outer(vi, vf)).astype(complex)]
+
+
+def _coherent_couplings(a, b, inter, dim, v_index):
+    """Coherent (Hamiltonian) couplings of one group interaction between
+    m_S states of two blocks (reference generate_generators.py:1503-1525 and
+    _couple_coherent_blocks :1961-1991): each entry of inter["coh"] couples
+    state `ini` of atom a with state `fin` of atom b at Rabi frequency `amp`
+    (rad/s); with "con" true it is controllable (label Vr, scaled by the
+    fourth coefficient, into Gr), else constant (Vc, into L0).  Entries
+    missing one of ini, fin, amp are skipped.  Returns ({label: operator},
+    next v_index); v_index counts couplings over all group interactions.
+    (The reference loses its count after an interaction between equal
+    spins that has no "rel" rate, and raises at the next coherent coupling;
+    the count here simply continues.)"""
+    out = {}
+    sa, sb = a.desc.get("S"), b.desc.get("S")
+    if sa is None or sb is None:
+        return out, v_index
+    for coh in inter.get("coh", []):
+        if not all(k in coh for k in ("ini", "fin", "amp")):
+            continue
+        label = "Vr" if coh.get("con") else "Vc"
+        Pi = a.ops["S" + _proj_key(sa, coh["ini"])]
+        Pf = b.ops["S" + _proj_key(sb, coh["fin"])]
+        for i, H in enumerate(_coherent(Pi, Pf, dim)):
+            out[f"{label} {v_index} {i}"] = H*coh["amp"]
+        v_index += 1
+    return out, v_index
+
+
+def _bell(qubit_b, qubit_c, singlet, rates, to_singlet):
+    """Jumps between a singlet and the Bell states of two spin-1/2 atoms b and
+    c of one block (reference _couple_bell_excited / _couple_bell_ground,
+    generate_generators.py:1796-1960): aligned (phi: ++, --) and
+    anti-aligned (psi: +-, -+) products of the atoms' projectors.  rates:
+    (psi rate, phi rate), None to skip; to_singlet: the jumps run from the
+    Bell states to the singlet (ground), else from the singlet (excited)."""
+    pb, mb = qubit_b.ops["S" + _proj_key(0.5, 0.5)], qubit_b.ops["S" + _proj_key(0.5, -0.5)]
+    pc, mc = qubit_c.ops["S" + _proj_key(0.5, 0.5)], qubit_c.ops["S" + _proj_key(0.5, -0.5)]
+    s = singlet.ops["S" + _proj_key(0, 0)]
+    states = {"psi+": pb*mc, "psi-": mb*pc, "phi+": pb*pc, "phi-": mb*mc}
+    dim = s.shape[0]
+    out = {}
+    for kind, rate in zip(("psi", "phi"), rates):
+        if rate is None:
+            continue
+        for sign in "+-":
+            proj = states[kind + sign]
+            jumps = _incoherent(proj, s, dim) if to_singlet else _incoherent(s, proj, dim)
+            for i, L in enumerate(jumps):
+                label = f"Lbell {kind}{sign} g {i}" if to_singlet else f"Lbell e {kind}{sign} {i}"
+                out[label] = L*math.sqrt(rate)
+    return out
+
+
+def _block_coupling(a, b, inter, dim, label_prefix, next_a=None, next_b=None):
+    """Jumps of one group interaction; returns {label: operator}.  next_a,
+    next_b: the atoms after a and b in their blocks (the second qubit of a
+    Bell pair), or None."""
     out = {}
     sa, sb = a.desc.get("S"), b.desc.get("S")
     if sa is None or sb is None:
         return out
-    if "coh" in inter:
-        raise NotImplementedError("coherent block couplings are not implemented")
 
     def P(atom, spin, m):
         return atom.ops["S" + _proj_key(spin, m)]
@@ -452,9 +529,20 @@ def _block_coupling(a, b, inter, dim, label_prefix):
                 continue
             for i, L in enumerate(_incoherent(P(a, 0, 0), P(b, 1, m), dim)):
                 out[f"Lisc{n} s {i}"] = L*np.sqrt(rate)
-    elif (sa == 0 and sb == 0.5) or (sa == 0.5 and sb == 0):
-        if any(k in inter for k in ("psi_gets_e", "phi_gets_e", "g_gets_psi", "g_gets_phi")):
-            raise NotImplementedError("Bell-state (hBN) couplings are not implemented")
+    elif sa == 0 and sb == 0.5:
+        # singlet a decays to the Bell states of atom b and the next atom
+        rates = (inter.get("psi_gets_e"), inter.get("phi_gets_e"))
+        if rates != (None, None):
+            if next_b is None:
+                raise ValueError("a Bell coupling needs the atom after the qubit in its block")
+            out.update(_bell(b, next_b, a, rates, to_singlet=False))
+    elif sa == 0.5 and sb == 0:
+        # the Bell states of atom a and the next atom decay to singlet b
+        rates = (inter.get("g_gets_psi"), inter.get("g_gets_phi"))
+        if rates != (None, None):
+            if next_a is None:
+                raise ValueError("a Bell coupling needs the atom after the qubit in its block")
+            out.update(_bell(a, next_a, b, rates, to_singlet=True))
     return out
 
 
@@ -481,9 +569,20 @@ def generate_atoms(description, atom_interactions, block_interactions, use_unita
                 if "|" not in k:
                     atom.ops[k] = _traceless(atom.ops[k])
         blocks.append((atoms, max(dim, 1), couplings))
+    # blocks joined by coherent couplings, closed transitively (generate_
+    # generators.py:76-91): their mutual coherences are allowed entries
+    nb = len(blocks)
+    joined = np.eye(nb, dtype=bool)
     for ((ba, _), (bb, _)), inter in block_interactions.items():
         if "coh" in inter:
-            raise NotImplementedError("coherent block couplings are not implemented")
+            joined[ba, bb] = joined[bb, ba] = True
+    while True:
+        grown = joined.copy()
+        for c in range(nb):
+            grown |= np.outer(joined[c], joined[c])
+        if (grown == joined).all():
+            break
+        joined = grown
     sizes = [d for _, d, _ in blocks]
     n = sum(sizes)
     offsets = np.cumsum([0] + sizes)
@@ -511,19 +610,32 @@ def generate_atoms(description, atom_interactions, block_interactions, use_unita
                 block_sum[k] = block_sum.get(k, 0) + Hj
         for k, M in block_sum.items():
             coherent[k] = coherent.get(k, 0) + embed(M, b)
+    couplings_h = {}
+    v_index = 0
     for ((ba, aa), (bb, ab)), inter in block_interactions.items():
-        atom_a = blocks[ba][0][aa]
-        atom_b = blocks[bb][0][ab]
-        for k, L in _block_coupling(atom_a, atom_b, inter, n, "").items():
+        atoms_a, atoms_b = blocks[ba][0], blocks[bb][0]
+        atom_a, atom_b = atoms_a[aa], atoms_b[ab]
+        hs, v_index = _coherent_couplings(atom_a, atom_b, inter, n, v_index)
+        for k, H in hs.items():
+            couplings_h[f"[{ba}, {aa}, {bb}, {ab}] {k}"] = H
+        nxt_a = atoms_a[aa + 1] if aa + 1 < len(atoms_a) else None
+        nxt_b = atoms_b[ab + 1] if ab + 1 < len(atoms_b) else None
+        for k, L in _block_coupling(atom_a, atom_b, inter, n, "", nxt_a, nxt_b).items():
             jumps[f"[{ba}, {aa}, {bb}, {ab}] {k}"] = L
 
     allowed = np.zeros((n, n), int)
-    for b in range(len(blocks)):
+    for b in range(nb):
         o = offsets[b]
         allowed[o:o + sizes[b], o:o + sizes[b]] = 1
+    for b1 in range(nb):
+        for b2 in range(nb):
+            if joined[b1, b2]:
+                allowed[offsets[b1]:offsets[b1 + 1], offsets[b2]:offsets[b2 + 1]] = 1
     if not use_incoherent:
         allowed[:] = 1
     valid = valid_indices_from_mask(allowed)
+    if use_unitary and not jumps and couplings_h:
+        raise NotImplementedError("unitary mode with coherent block couplings")
     if use_unitary and not jumps:
         # closed system: operator generators and the basis change matrices
         # (generate_generators.py:120-139); no superoperators
@@ -540,9 +652,11 @@ def generate_atoms(description, atom_interactions, block_interactions, use_unita
         supers[k] = dissipator(L, basis, sel)
     for k, H in coherent.items():
         supers[k] = von_neumann(H, basis, sel)
+    for k, H in couplings_h.items():
+        supers[k] = von_neumann(H, basis, sel)
     generators = _group(supers)
     return {"generators": generators, "super_all": supers, "coherent": coherent,
-            "jump": jumps, "allowed": allowed}, valid
+            "coherent_coupling": couplings_h, "jump": jumps, "allowed": allowed}, valid
 
 
 def _group(supers):

@@ -193,6 +193,41 @@ T1_END = 1/(2*10e-3*28e9)
 ZERO = const(0.0)
 
 
+def coherent_chain():
+    """A qubit, a qutrit and a qubit in three blocks joined by coherent
+    couplings: the first qubit's m = +1/2 to the qutrit's m = 0 at a
+    constant 30 MHz (Vc), the qutrit's m = 0 on to the second qubit's
+    m = -1/2 at 20 MHz times the fourth channel (Vr).  The qubits are joined only
+    through the qutrit, so their mutual coherences are allowed by the
+    transitive closure.  (The spins differ along the chain: the reference
+    numbers the couplings wrongly after a coupling between equal spins
+    that has no "rel" rate, and raises at the next one.)"""
+    spins = [[{"S": 1/2, "g": 2.0, "B0": B0}],
+             [{"S": 1, "g": -1/2, "D": 72, "B0": B0}],
+             [{"S": 1/2, "g": 2.0, "B0": B0}]]
+    groups = {
+        ((0, 0), (1, 0)): {"coh": [{"ini": 1/2, "fin": 0, "amp": math.tau*30e6}]},
+        ((1, 0), (2, 0)): {"coh": [{"ini": 0, "fin": -1/2, "amp": math.tau*20e6,
+                                    "con": True}]},
+    }
+    return spins, [{}, {}, {}], groups
+
+
+def hbn_bell():
+    """A pair of spin-1/2 atoms in one block (a hBN-like triplet pair) and a
+    singlet block: the singlet decays into the Bell states of the pair
+    (psi at 20 /us, phi at 10 /us) and the pair decays back (psi at 3 /us,
+    phi at 1 /us)."""
+    pair = [{"S": 1/2, "g": 2.0, "B0": B0, "TS2": 1e-6},
+            {"S": 1/2, "g": 2.0, "B0": B0}]
+    spins = [pair, [{"S": 0}]]
+    groups = {
+        ((1, 0), (0, 0)): {"psi_gets_e": 2e7, "phi_gets_e": 1e7},
+        ((0, 0), (1, 0)): {"g_gets_psi": 3e6, "g_gets_phi": 1e6},
+    }
+    return spins, [{}, {}], groups
+
+
 def cases():
     q_drive = drive(28e6, 10e-6)
     t_drive = drive(7e6, 10e-6)
@@ -267,6 +302,17 @@ def cases():
              ch=[c1_drive, ZERO, ZERO, ZERO], rho0=rho_c1,
              t=(0, 1e-9, 1e-9), rot=False, res=True, K=2, F=100,
              use_incoherent=False),
+        dict(name="coherent_chain", csv=None, spins=coherent_chain()[0],
+             spin_interactions=coherent_chain()[1],
+             group_interactions=coherent_chain()[2],
+             ch=[q_drive, ZERO, ZERO, const(0.5)],
+             rho0=np.diag([1.0, 0, 0, 0, 0, 0, 0]).astype(complex),
+             t=(0, 4e-9, 1e-9), rot=False, res=True, K=2, F=10, path="cpu"),
+        dict(name="hbn_bell", csv=None, spins=hbn_bell()[0],
+             spin_interactions=hbn_bell()[1], group_interactions=hbn_bell()[2],
+             ch=[q_drive, ZERO, ZERO, ZERO],
+             rho0=np.diag([0.0, 0, 0, 0, 1.0]).astype(complex),
+             t=(0, 10e-9, 1e-9), rot=False, res=True, K=2, F=20, path="cpu"),
         dict(name="qutrit_hyperfine", csv="qutrit-hyperfine",
              spins=QUTRIT_HF, ch=[t_drive, ZERO, ZERO, ZERO],
              rho0=np.diag([1.0, 0, 0, 0, 0, 0]).astype(complex),

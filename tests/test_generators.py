@@ -120,3 +120,45 @@ def test_nv21_model_matches_reference():
     for i, k in enumerate(LABELS):
         ref = z["generators"][i]
         assert np.abs(g["generators"][k] - ref).max() <= 1e-15*np.abs(ref).max()
+
+
+def test_coherent_couplings_labels_and_closure():
+    """Coherent block couplings: one Hermitian operator per coupled state
+    pair, labelled Vc (constant, into L0) or Vr (into Gr) with the running
+    coupling index; blocks 0 and 2, joined only through block 1, have their
+    coherences allowed by the transitive closure, and an uncoupled fourth
+    block does not."""
+    spins, inter, groups = make_golden.coherent_chain()
+    ops, vm = generate_atoms(spins, inter, groups)
+    hs = ops["coherent_coupling"]
+    assert sorted(hs) == ["[0, 0, 1, 0] Vc 0 0", "[1, 0, 2, 0] Vr 1 0"]
+    for H in hs.values():
+        assert np.array_equal(H, H.conj().T) and np.count_nonzero(H) == 2
+    allowed = ops["allowed"]
+    assert allowed.shape == (7, 7) and allowed.all()
+    # an extra uncoupled qubit block: its coherences with the chain stay out
+    ops4, vm4 = generate_atoms(spins + [[{"S": 1/2, "g": 2.0, "B0": make_golden.B0}]],
+                               inter + [{}], groups)
+    a4 = ops4["allowed"]
+    assert a4[:7, :7].all() and not a4[:7, 7:].any() and a4[7:, 7:].all()
+    # the Vr coupling is the only controllable term: Gr is exactly its
+    # von Neumann superoperator
+    assert np.abs(ops["generators"]["Gr"]).max() > 0
+
+
+def test_bell_couplings_labels():
+    """hBN-style Bell couplings: the singlet decays to each of the four Bell
+    product states of the pair and back, sqrt(rate) scaled jumps."""
+    spins, inter, groups = make_golden.hbn_bell()
+    ops, _ = generate_atoms(spins, inter, groups)
+    labels = sorted(k.split("] ", 1)[1] for k in ops["jump"] if "Lbell" in k)
+    want = sorted([f"Lbell e {s} 0" for s in ("psi+", "psi-", "phi+", "phi-")] +
+                  [f"Lbell {s} g 0" for s in ("psi+", "psi-", "phi+", "phi-")])
+    assert labels == want
+    L = ops["jump"]["[1, 0, 0, 0] Lbell e psi+ 0"]
+    assert np.isclose(np.abs(L).max(), np.sqrt(2e7))
+    L = ops["jump"]["[0, 0, 1, 0] Lbell phi- g 0"]
+    assert np.isclose(np.abs(L).max(), np.sqrt(1e6))
+    with pytest.raises(ValueError):
+        # the pair's second atom is missing
+        generate_atoms([[spins[0][0]], spins[1]], [{}, {}], groups)

@@ -12,7 +12,7 @@ CASES = ["qubit_couple_res_e2", "qubit_couple_res_e5", "qubit_couple_res_e3_e6",
          "qubit_t1_0K", "qubit_t1_mK", "qutrit_couple", "qutrit_couple_unital",
          "qubit_hyperfine", "qubit_couple_rot_e5", "spin1_c1", "nv7_n49",
          "nv7_n19", "qubit_couple_nh", "qubit_couple_rot_nh", "qubit_t1_0K_rot",
-         "qubit_t1_mK_rot_e2"]
+         "qubit_t1_mK_rot_e2", "coherent_chain", "hbn_bell"]
 NONRES = ["qubit_couple", "qubit_couple_rot_e1_nores"]
 
 
@@ -137,7 +137,7 @@ def _case_by_name(name):
 
 @pytest.mark.parametrize("name", ["qubit_couple_res_e2", "qubit_t1_mK", "qutrit_couple",
                                   "qubit_hyperfine", "qubit_couple_rot_e5", "spin1_c1",
-                                  "qubit_couple_rot_nh"])
+                                  "qubit_couple_rot_nh", "coherent_chain", "hbn_bell"])
 def test_simspins_front_end_matches_reference(name):
     """The whole front end -- this package's generator builder, rotating
     frame and simulator -- against the reference's simspins output."""

@@ -15,7 +15,7 @@ CASES = ["qubit_couple", "qubit_couple_res_e2", "qubit_couple_res_e2_cpu",
          "qubit_hyperfine", "qubit_couple_rot_e5",
          "qubit_couple_rot_e1_nores", "spin1_c1", "nv7_n49", "nv7_n19",
          "qubit_couple_nh", "qubit_couple_rot_nh", "qubit_t1_0K_rot",
-         "qubit_t1_mK_rot_e2"]
+         "qubit_t1_mK_rot_e2", "coherent_chain", "hbn_bell"]
 
 
 def vmap(c):
