@@ -557,6 +557,8 @@ def main():
             kernel_ms.append(0.0 if n_chunks else plan.batch_info()["kernel_ms"])
         barrier(world)
         clock_info = clocks.stop()
+    # every readout the timed steps wrote was finite (raises otherwise)
+    plan.batch_check(stream.cuda_stream)
     info = plan.batch_info()
     launches = (n_chunks or plan.last_launches())*args.steps
     total_ms = max_over_ranks(sum(times), world)
@@ -621,7 +623,12 @@ def main():
                        "autotune": None if tuned is None else {
                            "chosen": {"lanes": tuned["config"][0], "variant": tuned["config"][1],
                                       "cta_threads": tuned["config"][2]},
-                           "trials": len(tuned["trials"])},
+                           "trials": len(tuned["trials"]),
+                           "samples_per_launch": tuned["samples_per_launch"],
+                           "launch_length_trials": {
+                               str(t["samples_per_launch"]): round(t["ms_per_traj_step"]*1e9, 4)
+                               for t in tuned["chunk_trials"]},
+                           "launch_length_unit": "ns per traj-step over a 64-sample window"},
                        "kernel": {"lanes": info["lanes"], "taylor_degree": info["degree"],
                                   "substeps": info["substeps"], "rows": info["rows"],
                                   "nnz": info["nnz"], "variant": info["variant"],

@@ -141,7 +141,12 @@ int sss_simulate_device(sss_plan* plan, int ntraj, const double* rho0, int nch,
  * set) runs in the generalised rotating frame on the row-part kernel
  * (variant 0 or 4): states, weights and outputs stay in the lab basis, the
  * kernel converting with V and V^-1 (generate_simulator.py:450-532 Omega,
- * :901-1021 e^{L0 h} blocks, :2030-2038 sandwich). */
+ * :901-1021 e^{L0 h} blocks, :2030-2038 sandwich).
+ * Health check (the reference has none): the kernels test every readout
+ * and final-state value they write and record the first NaN or infinity
+ * in a device word.  With host != 0 the call returns SSS_ENONFINITE
+ * (naming the trajectory and output sample) when one was written; with
+ * host == 0 the call stays asynchronous and sss_batch_check reports it. */
 int sss_batch_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                   int nseg, const double* programs, const int* samples,
                   double t0, double dt, int T_max, int F,
@@ -205,6 +210,12 @@ int sss_batch_prepare_samples(sss_plan* plan, int ntraj, const double* rho0,
 int sss_batch_launch(sss_plan* plan, double* state, const double* programs,
                      const int* samples, double t0, int t_begin, int n_samples,
                      int T_max, double* readout, void* cuda_stream);
+/* Synchronises cuda_stream and reads the health word of the prepared batch:
+ * SSS_ENONFINITE if a launch (or device-pointer sss_batch_run) since the
+ * last prepare or check wrote a NaN or infinite readout or final-state
+ * value (the word is then reset), else SSS_OK.  Call it after the last
+ * chunk of a run, or after replaying a captured graph of launches. */
+int sss_batch_check(sss_plan* plan, void* cuda_stream);
 
 /* Adjoint gradients (no reference counterpart: the reference computes no
  * derivatives).  For each trajectory, the objective
@@ -226,6 +237,26 @@ int sss_adjoint_run(sss_plan* plan, int ntraj, const double* rho0, int nch,
                     int T, int F, const double* readout_weights,
                     const double* time_weights, double* J, double* grad,
                     int host, void* cuda_stream);
+
+/* sss_adjoint_run for the segments of any program channel, with four
+ * parameters per segment: channel c (0 <= c < nch, generator G_{c+1}; 3 is
+ * the fourth channel, e.g. the laser power) and
+ *   grad[((b*nseg + s)*4 + 0]  dJ/d amplitude_s
+ *   grad[((b*nseg + s)*4 + 1]  dJ/d phase_s
+ *   grad[((b*nseg + s)*4 + 2]  dJ/d offset_s
+ *   grad[((b*nseg + s)*4 + 3]  dJ/d frequency_s
+ * of c(t) = offset_s + amplitude_s cos(2 pi frequency_s t + phase_s).  The
+ * other channels are held fixed.  SSS_EINVAL when the channel has no
+ * generator or its generator is zero on the rows reachable from rho0;
+ * with host != 0, SSS_ENONFINITE when J or a gradient entry is NaN or
+ * infinite.  sss_adjoint_run is channel 0 with the first two entries. */
+int sss_adjoint_run_channel(sss_plan* plan, int ntraj, const double* rho0,
+                            int nch, int nseg, const double* programs,
+                            double t0, double dt, int T, int F,
+                            const double* readout_weights,
+                            const double* time_weights, int channel,
+                            double* J, double* grad, int host,
+                            void* cuda_stream);
 
 /* Equivalence-class ("kernel") mode.  The plan's generators act on the
  * r = N dimensional image of the orthonormal basis P (n_full x N, row-major),

@@ -25,8 +25,8 @@ SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_simulate_device", "sss_batch_run", "sss_batch_run_table", "sss_plan_last_launches",
            "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
            "sss_plan_set_projection", "sss_plan_set_unitary",
-           "sss_fp64_peak", "sss_fp64_mma_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_batch_prepare",
-           "sss_batch_prepare_samples", "sss_batch_launch", "sss_slot_layout", "sss_plan_batch_work", "sss_last_error",
+           "sss_fp64_peak", "sss_fp64_mma_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_adjoint_run_channel", "sss_batch_prepare",
+           "sss_batch_prepare_samples", "sss_batch_launch", "sss_batch_check", "sss_slot_layout", "sss_plan_batch_work", "sss_last_error",
            "sss_plan_destroy"]
 
 
@@ -88,12 +88,17 @@ def load(build_if_missing=True):
         L.sss_fp64_mma_peak.restype = i
         L.sss_adjoint_run.argtypes = [vp, i, vp, i, i, vp, d, d, i, i, dp, dp, vp, vp, i, vp]
         L.sss_adjoint_run.restype = i
+        L.sss_adjoint_run_channel.argtypes = [vp, i, vp, i, i, vp, d, d, i, i, dp, dp, i, vp, vp,
+                                              i, vp]
+        L.sss_adjoint_run_channel.restype = i
         L.sss_batch_prepare.argtypes = [vp, i, vp, i, i, vp, d, i, dp, vp]
         L.sss_batch_prepare.restype = i
         L.sss_batch_prepare_samples.argtypes = [vp, i, vp, i, i, vp, vp, d, i, dp, vp]
         L.sss_batch_prepare_samples.restype = i
         L.sss_batch_launch.argtypes = [vp, vp, vp, vp, d, i, i, i, vp, vp]
         L.sss_batch_launch.restype = i
+        L.sss_batch_check.argtypes = [vp, vp]
+        L.sss_batch_check.restype = i
         L.sss_fp64_peak.restype = i
         L.sss_slot_layout.argtypes = [i, ip, ip, i, i, ip, ip, ip,
                                       ctypes.POINTER(ctypes.c_uint), ip]
@@ -295,6 +300,27 @@ class Plan:
             grad.ctypes.data_as(ctypes.c_void_p), 1, stream))
         return J, grad
 
+    def adjoint_channel(self, rho0, programs, t0, dt, T, F, readout_weights, time_weights,
+                        channel, stream=None):
+        """Host-buffer adjoint run for the segments of one channel.  Returns
+        (J (B,), grad (B, nseg, 4)): d/d (amplitude, phase, offset,
+        frequency) of every segment of `channel`."""
+        rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
+        programs = np.ascontiguousarray(programs, dtype=np.float64)
+        B = rho0.shape[0]
+        nch, nseg = programs.shape[1], programs.shape[2]
+        J = np.empty(B)
+        grad = np.empty((B, nseg, 4))
+        rw = np.ascontiguousarray(readout_weights, dtype=np.float64)
+        tw = np.ascontiguousarray(time_weights, dtype=np.float64)
+        assert tw.size == T
+        check(load().sss_adjoint_run_channel(
+            self._h, B, rho0.ctypes.data_as(ctypes.c_void_p), nch, nseg,
+            programs.ctypes.data_as(ctypes.c_void_p), float(t0), float(dt), int(T), int(F),
+            dptr(rw), dptr(tw), int(channel), J.ctypes.data_as(ctypes.c_void_p),
+            grad.ctypes.data_as(ctypes.c_void_p), 1, stream))
+        return J, grad
+
     def batch_prepare(self, rho0_ptr, B, programs_ptr, nch, nseg, dt, F,
                       readout_weights=None, stream=None, samples=None):
         """Analyse a batch (device pointers) and upload the kernel tables.
@@ -318,6 +344,11 @@ class Plan:
         check(load().sss_batch_launch(self._h, state_ptr, programs_ptr, samples_ptr, float(t0),
                                       int(t_begin), int(n_samples), int(T_max), readout_ptr,
                                       stream))
+
+    def batch_check(self, stream=None):
+        """Wait for the stream; raise SSSError (ENONFINITE) if a launch since
+        the last prepare or check wrote a NaN or infinite value."""
+        check(load().sss_batch_check(self._h, stream))
 
     def set_batch_config(self, lanes=0, cta_threads=0, variant=0):
         check(load().sss_plan_set_batch_config(self._h, int(lanes), int(cta_threads),

@@ -3,7 +3,9 @@
 ``sss_adjoint_run`` (libsss.so) computes, for a batch of trajectories, the
 objective J = sum_t tw[t] * rw . rho(t) -- e.g. integrated fluorescence --
 and its gradient with respect to the amplitude and phase of every segment
-of the x-drive channel, by an adjoint sweep on the GPU: the forward pass
+of the x-drive channel (``sss_adjoint_run_channel``: amplitude, phase,
+offset and frequency of the segments of any channel, such as a detuned y
+drive or the laser power), by an adjoint sweep on the GPU: the forward pass
 stores the state before every exponential when device memory allows it
 (trajectories in memory-sized chunks) and the backward pass walks the
 stored states; when one trajectory's states do not fit, a checkpointed
@@ -44,11 +46,16 @@ class Objective:
         W, nodes = method(number_of_exponentials)
         self.plan = _lib.Plan(self.gens, W, nodes)
 
-    def run(self, programs, dt, T, time_weights):
+    def run(self, programs, dt, T, time_weights, channel=None):
         """J (B,) and gradient (B, nseg, 2) w.r.t. (amplitude [program
-        units], phase) of every x-channel segment."""
+        units], phase) of every x-channel segment; with `channel`, the
+        gradient (B, nseg, 4) w.r.t. (amplitude, phase, offset, frequency)
+        of that channel's segments."""
         B = programs.shape[0]
         rho0 = np.repeat(self.rho0[None], B, axis=0)
+        if channel is not None:
+            return self.plan.adjoint_channel(rho0, programs, 0.0, dt, T, self.F, self.rw,
+                                             time_weights, channel)
         return self.plan.adjoint(rho0, programs, 0.0, dt, T, self.F, self.rw, time_weights)
 
     def forward_only(self, programs, dt, T, time_weights):

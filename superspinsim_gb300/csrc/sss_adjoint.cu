@@ -1,13 +1,17 @@
 // Adjoint gradients of a time-integrated readout with respect to the
-// amplitudes and phases of the x-drive segments.  No reference
-// counterpart: the reference has no derivatives.  The forward model is the
+// parameters of one channel's segments (by default the x drive's
+// amplitudes and phases).  No reference counterpart: the reference has no
+// derivatives.  The forward model is the
 // reference's integrator exactly as the batched kernel runs it
 // (superspinsim/generate_simulator.py:1954-2015 step structure, CF weights
 // :278-350, exponential K-1 first :1259-1294).
 //
 // Objective (per trajectory):  J = sum_t tw[t] * rw . rho(t0 + dt*(t+1)).
-// Parameters: for every segment s of channel 0 (the x field), its amplitude
-// a_s and phase phi_s (c_x(t) = offset + a_s cos(tau f t + phi_s)).
+// Parameters: for every segment s of the differentiated channel c (channel
+// 0, the x field, by default), its amplitude a_s and phase phi_s, and with
+// four parameters also its offset o_s and frequency f_s
+// (c(t) = o_s + a_s cos(tau f_s t + phi_s)).  Below, Gx stands for that
+// channel's generator G_{c+1}.
 //
 // Every parameter enters a step's exponent Omega_e only through the scalar
 // coefficient of Gx, so dOmega_e/dtheta = beta_e(theta) Gx with
@@ -53,6 +57,7 @@ constexpr int kAdjMaxTaylor = 24;
 struct AdjArgs {
     int M, Ga, K, Q, F, nch, nseg, ntraj, degree, N, E, ET;
     int xg;          // position of Gx among the active generators
+    int dch, npar;   // differentiated channel; parameters per segment (2 or 4)
     long n_steps;    // fine steps per trajectory
     int T, C, n_ck;
     double h, t0, dt;
@@ -73,7 +78,7 @@ struct AdjArgs {
     const double* rho0;     // ntraj*N
     const double* prog;     // ntraj*nch*nseg*5
     double* J;              // ntraj
-    double* grad;           // ntraj*nseg*2
+    double* grad;           // ntraj*nseg*npar
     double* ck;             // slots*n_ck*M
     double* st;             // slots*C*K*M
     int* queue;
@@ -86,7 +91,8 @@ __device__ __forceinline__ int wend(unsigned w) { return (int)(w >> 16); }
 // transposed-entry index flag: the x generator is non-zero at this entry
 constexpr int kHasG = 1 << 30;
 
-// x-channel segment at time t: index (or -1) and its parameters
+// segment of a channel's program (prog points at the channel) at time t,
+// or -1 past its last segment
 __device__ __forceinline__ int x_segment(const double* prog, int nseg, double t) {
     for (int s = 0; s < nseg; s++)
         if (t < prog[s * 5]) return s;
@@ -237,10 +243,11 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
             double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + r)),
                                             __dmul_rn(a.dt, (double)t)),
                                   __ldg(a.noff + k));
-            int s = x_segment(prog, a.nseg, tn);
+            const double* dprog = prog + (size_t)a.dch * a.nseg * 5;
+            int s = x_segment(dprog, a.nseg, tn);
             double cs = 0.0, dph = 0.0;
             if (s >= 0) {
-                const double* p = prog + s * 5;
+                const double* p = dprog + s * 5;
                 double arg = __dadd_rn(__dmul_rn(__dmul_rn(6.283185307179586, p[3]), tn), p[4]);
                 double sn, cn;
                 sincos(arg, &sn, &cn);
@@ -250,6 +257,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
             nd[4 * k] = cs;
             nd[4 * k + 1] = dph;
             nd[4 * k + 2] = (double)s;
+            nd[4 * k + 3] = dph * (6.283185307179586 * tn);  // d c / d frequency
         }
         grp.sync();
     };
@@ -287,7 +295,6 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
         const int b = __shfl_sync(grp.gmask, nb, grp.leader);
         if (b >= a.ntraj) break;
         const double* prog = a.prog + (size_t)b * a.nch * a.nseg * 5;
-        const double* xprog = prog;  // channel 0 = x
         // ---- forward with checkpoints ----
         for (int i = grp.r0; i < grp.r1; i++) v[i] = a.rho0[(size_t)b * a.N + a.row_orig[i]];
         grp.sync();
@@ -308,9 +315,9 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
             }
         }
         if (li == 0) a.J[b] = Jacc;
-        double* gb = a.grad + (size_t)b * a.nseg * 2;
+        double* gb = a.grad + (size_t)b * a.nseg * a.npar;
         if (li == 0)
-            for (int s = 0; s < 2 * a.nseg; s++) gb[s] = 0.0;
+            for (int s = 0; s < a.npar * a.nseg; s++) gb[s] = 0.0;
         // ---- backward ----
         for (int i = grp.r0; i < grp.r1; i++) mu[i] = 0.0;
         grp.sync();
@@ -369,15 +376,19 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
                             int sgm = (int)nd[4 * k + 2];
                             if (sgm < 0) continue;
                             double hw = a.h * __ldg(a.W + e * Q + k);
-                            gb[2 * sgm] = fma(hw * nd[4 * k], g, gb[2 * sgm]);
-                            gb[2 * sgm + 1] = fma(hw * nd[4 * k + 1], g, gb[2 * sgm + 1]);
+                            double* gs = gb + (size_t)a.npar * sgm;
+                            gs[0] = fma(hw * nd[4 * k], g, gs[0]);
+                            gs[1] = fma(hw * nd[4 * k + 1], g, gs[1]);
+                            if (a.npar == 4) {
+                                gs[2] = fma(hw, g, gs[2]);
+                                gs[3] = fma(hw * nd[4 * k + 3], g, gs[3]);
+                            }
                         }
                     }
                     grp.sync();
                 }
             }
         }
-        (void)xprog;
     }
 }
 
@@ -410,6 +421,7 @@ struct AdjPartsArgs {
     long n_steps;
     double h, t0, dt;
     int n_live, x_live, kc, ngx;
+    int dch, npar;          // differentiated channel; parameters per segment (2 or 4)
     int live[kMaxG];
     int gen_index[kMaxG];
     const int* pcol;        // C*P*L transposed entry columns [e][l]
@@ -441,13 +453,13 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
     const int Ms = M + 2;  // rows, the zero row M, the sink row M+1
     const int slot = threadIdx.x / L, li = threadIdx.x % L;
     const size_t per_slot =
-        (6 * (size_t)Ms + 2 * (size_t)(L * C + 1) + (size_t)kRing * (Q * NL + K * NL + 3 * Q)) | 1;
+        (6 * (size_t)Ms + 2 * (size_t)(L * C + 1) + (size_t)kRing * (Q * NL + K * NL + 4 * Q)) | 1;
     double* sb = smem + slot * per_slot;
     double* parts1 = sb + 6 * (size_t)Ms;
     double* parts2 = parts1 + L * C + 1;
     double* ringc = parts2 + L * C + 1;         // [s][k][live] node values
     double* ring_ag = ringc + kRing * Q * NL;   // [s][e][live] CF weights
-    double* ring_d = ring_ag + kRing * K * NL;  // [s][k][3] cos, -a sin, segment of the x channel
+    double* ring_d = ring_ag + kRing * K * NL;  // [s][k][4] cos, -a sin, segment, -a sin tau t
     double* s_rw = smem + (size_t)(blockDim.x / L) * per_slot;
     for (int i = threadIdx.x; i < M; i += blockDim.x) s_rw[i] = a.rw[i];
     for (int i = li; i < 6 * Ms; i += L) sb[i] = 0.0;
@@ -518,15 +530,18 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
             s = gsum(s);
             if (li == 0) a.J[b] = s;
         }
-        double* gb = a.grad + (size_t)b * a.nseg * 2;
+        const double* dprog = prog + (size_t)a.dch * a.nseg * 5;
+        double* gb = a.grad + (size_t)b * a.nseg * a.npar;
         // lane 0: running gradient sums per node, for segment cur_seg[k]
         int cur_seg[kMaxQ];
-        double acc_a[kMaxQ], acc_p[kMaxQ];
+        double acc_a[kMaxQ], acc_p[kMaxQ], acc_o[kMaxQ], acc_f[kMaxQ];
 #pragma unroll
         for (int k = 0; k < kMaxQ; k++) {
             cur_seg[k] = -1;
             acc_a[k] = 0.0;
             acc_p[k] = 0.0;
+            acc_o[k] = 0.0;
+            acc_f[k] = 0.0;
         }
         for (int row = r0; row < r1; row++) mu[row] = 0.0;
         gsync();
@@ -540,11 +555,12 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
             }
             if (rp == kRing) {
                 // steps n, n-1, ..., n-kRing+1: node values of the live channels;
-                // for the x channel also cos, -a sin and the segment
+                // for the differentiated channel also cos, -a sin, the segment
+                // and -a sin tau t
                 for (int i = li; i < kRing * Q * NL; i += L) {
                     const int s = i / (Q * NL), rem = i - s * Q * NL, k = rem / NL, gi = rem - k * NL;
                     const long ns = n - s;
-                    double val = 0.0, cs = 0.0, dph = 0.0;
+                    double val = 0.0, cs = 0.0, dph = 0.0, dfr = 0.0;
                     int sg = -1;
                     if (ns >= 0) {
                         const int ts = (int)(ns / a.F), rs = (int)(ns % a.F);
@@ -553,13 +569,14 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                                                     __ldg(a.noff + k));
                         const int g = a.gen_index[a.live[gi]];
                         if (gi == a.x_live) {
-                            sg = x_segment(prog, a.nseg, tn);
+                            sg = x_segment(dprog, a.nseg, tn);
                             if (sg >= 0) {
-                                const double* q = prog + sg * 5;
+                                const double* q = dprog + sg * 5;
                                 const double arg =
                                     __dadd_rn(__dmul_rn(__dmul_rn(6.283185307179586, q[3]), tn), q[4]);
                                 cs = cos(arg);
                                 dph = -q[2] * sin(arg);
+                                dfr = dph * (6.283185307179586 * tn);
                                 val = q[2] == 0.0 ? q[1] : __dadd_rn(q[1], __dmul_rn(q[2], cs));
                             }
                         } else {
@@ -568,10 +585,11 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                     }
                     ringc[i] = val;
                     if (gi == a.x_live) {
-                        double* rd = ring_d + (s * Q + k) * 3;
+                        double* rd = ring_d + (s * Q + k) * 4;
                         rd[0] = cs;
                         rd[1] = dph;
                         rd[2] = (double)sg;
+                        rd[3] = dfr;
                     }
                 }
                 gsync();
@@ -654,21 +672,30 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
 #pragma unroll
                     for (int k = 0; k < kMaxQ; k++) {
                         if (k >= Q) break;
-                        const double* rd = ring_d + (rp * Q + k) * 3;
+                        const double* rd = ring_d + (rp * Q + k) * 4;
                         const int sg = (int)rd[2];
                         if (sg != cur_seg[k]) {
                             if (cur_seg[k] >= 0) {
-                                gb[2 * cur_seg[k]] += acc_a[k];
-                                gb[2 * cur_seg[k] + 1] += acc_p[k];
+                                double* gs = gb + (size_t)a.npar * cur_seg[k];
+                                gs[0] += acc_a[k];
+                                gs[1] += acc_p[k];
+                                if (a.npar == 4) {
+                                    gs[2] += acc_o[k];
+                                    gs[3] += acc_f[k];
+                                }
                             }
                             cur_seg[k] = sg;
                             acc_a[k] = 0.0;
                             acc_p[k] = 0.0;
+                            acc_o[k] = 0.0;
+                            acc_f[k] = 0.0;
                         }
                         if (sg >= 0) {
                             const double hw = a.h * __ldg(a.W + e_exp * Q + k);
                             acc_a[k] = fma(hw * rd[0], g, acc_a[k]);
                             acc_p[k] = fma(hw * rd[1], g, acc_p[k]);
+                            acc_o[k] = fma(hw, g, acc_o[k]);
+                            acc_f[k] = fma(hw * rd[3], g, acc_f[k]);
                         }
                     }
                 }
@@ -680,8 +707,13 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
 #pragma unroll
             for (int k = 0; k < kMaxQ; k++)
                 if (k < Q && cur_seg[k] >= 0) {
-                    gb[2 * cur_seg[k]] += acc_a[k];
-                    gb[2 * cur_seg[k] + 1] += acc_p[k];
+                    double* gs = gb + (size_t)a.npar * cur_seg[k];
+                    gs[0] += acc_a[k];
+                    gs[1] += acc_p[k];
+                    if (a.npar == 4) {
+                        gs[2] += acc_o[k];
+                        gs[3] += acc_f[k];
+                    }
                 }
         }
         gsync();
@@ -716,19 +748,22 @@ int launch_adj_parts(sss_plan* p, int C, int P, const AdjPartsArgs& a, int threa
 // row-part kernels or the states of one trajectory do not fit in memory.
 int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                       const double* d_prog, double t0, double dt, int T, int F,
-                      const double* h_rw, const double* h_tw, double* d_J, double* d_grad,
-                      cudaStream_t st) {
+                      const double* h_rw, const double* h_tw, int dch, int npar, double* d_J,
+                      double* d_grad, cudaStream_t st) {
     const int N = p->d.N, K = p->d.K, Q = p->d.Q;
+    const int gd = dch + 1;  // the differentiated channel's generator
     BatchLayout Ly;
-    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {1}, true, &Ly, st, true))
+    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {gd}, true, &Ly, st, true))
         return rc;
     if (Ly.M == 0) return fail(SSS_EINVAL, "empty pattern");
     if (Ly.substeps != 1) return fail(SSS_EINVAL, "the adjoint needs one sub-step per exponential");
     if (Ly.degree > kAdjMaxTaylor) return fail(SSS_EINVAL, "Taylor degree too large for the adjoint");
     int xg = -1;
     for (int gi = 0; gi < Ly.Ga; gi++)
-        if (Ly.active[gi] == 1) xg = gi;
-    if (xg < 0) return fail(SSS_EINVAL, "the x generator is zero on the reachable rows");
+        if (Ly.active[gi] == gd) xg = gi;
+    if (xg < 0)
+        return fail(SSS_EINVAL, "the generator of channel " + std::to_string(dch) +
+                                    " is zero on the reachable rows");
     const int M = Ly.M, Ga = Ly.Ga;
     const long n_steps = (long)T * F;
     const size_t per_traj = sizeof(double) * (size_t)n_steps * K * M;
@@ -747,7 +782,7 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
     for (int i = 0; i < M; i++)
         for (const BatchLayout::Ent& en : Ly.row_ents[i]) {
             rowsT[en.col].push_back({i, en.q});
-            prioT[en.col].push_back(sp.val[(size_t)1 * sp.nnz + en.q] != 0.0);
+            prioT[en.col].push_back(sp.val[(size_t)gd * sp.nnz + en.q] != 0.0);
         }
     BatchLayout TL;
     // lanes of the backward groups: the narrowest that fits and gives every
@@ -773,9 +808,9 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
         return rc;
     const int CP = TL.C * TL.P;
 
-    // ---- forward tables (x channel kept live) ----
+    // ---- forward tables (the differentiated channel kept live) ----
     PartsForward fw;
-    if (int rc = parts_forward_prepare(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {1}, p->w_adjf, &fw, st))
+    if (int rc = parts_forward_prepare(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {gd}, p->w_adjf, &fw, st))
         return rc;
 
     // ---- backward tables ----
@@ -784,7 +819,7 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
     std::vector<double> om0((size_t)K * CP * Lb, 0.0);
     for (int gi = 0; gi < Ga; gi++) {
         const int g = Ly.active[gi];
-        if (g != 0 && (g == 1 || !Ly.chan_const[g])) {
+        if (g != 0 && (g == gd || !Ly.chan_const[g])) {
             live.push_back(gi);
             continue;
         }
@@ -847,6 +882,8 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
     a.n_steps = n_steps; a.h = h; a.t0 = t0; a.dt = dt;
     a.n_live = (int)live.size();
     a.x_live = x_live;
+    a.dch = dch;
+    a.npar = npar;
     a.kc = TL.kc;
     a.ngx = ngx;
     for (size_t i = 0; i < live.size(); i++) a.live[i] = live[i];
@@ -866,7 +903,7 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
     for (int j = 0; j <= kAdjMaxTaylor; j++) a.inv_j[j] = j ? 1.0 / j : 0.0;
     const size_t smem = sizeof(double) *
         (((6 * (size_t)(M + 2) + 2 * (size_t)(Lb * TL.C + 1) +
-           (size_t)kRing * (Q * live.size() + K * live.size() + 3 * Q)) | 1) * (threads / Lb) + M);
+           (size_t)kRing * (Q * live.size() + K * live.size() + 4 * Q)) | 1) * (threads / Lb) + M);
     if (smem > 227 * 1024) return fail(SSS_EINVAL, "adjoint kernel: shared memory per CTA too large");
 
     // ---- buffers and chunks ----
@@ -875,7 +912,7 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
     if (int rc = p->w_adjst.ensure(sizeof(double) * (size_t)chunk * N)) return rc;
     if (int rc = p->w_queue.ensure(sizeof(int) * 4)) return rc;
     SSS_CUDA(cudaMemsetAsync(d_J, 0, sizeof(double) * ntraj, st));
-    SSS_CUDA(cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ntraj * nseg * 2, st));
+    SSS_CUDA(cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ntraj * nseg * npar, st));
     if (!p->ev_begin) {
         SSS_CUDA(cudaEventCreate(&p->ev_begin));
         SSS_CUDA(cudaEventCreate(&p->ev_end));
@@ -897,7 +934,7 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
         ab.readout = p->w_adjro.as<double>();
         ab.prog = prog;
         ab.J = d_J + b0;
-        ab.grad = d_grad + (size_t)b0 * nseg * 2;
+        ab.grad = d_grad + (size_t)b0 * nseg * npar;
         ab.queue = p->w_queue.as<int>();
         SSS_CUDA(cudaMemsetAsync(ab.queue, 0, sizeof(int), st));
         int rc;
@@ -927,27 +964,34 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
 
 int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 const double* d_prog, double t0, double dt, int T, int F, const double* h_rw,
-                const double* h_tw, double* d_J, double* d_grad, cudaStream_t st) {
+                const double* h_tw, int dch, int npar, double* d_J, double* d_grad,
+                cudaStream_t st) {
+    if (dch < 0 || dch >= nch || dch + 1 >= p->d.G)
+        return fail(SSS_EINVAL, "the differentiated channel must be a program channel with a "
+                                "generator (0 <= channel < nch, channel + 1 < G)");
+    if (npar != 2 && npar != 4) return fail(SSS_EINVAL, "parameters per segment must be 2 or 4");
     if (p->batch_variant == 0 || p->batch_variant == 4 || p->batch_variant == 5) {
         const int rc = adjoint_run_parts(p, ntraj, d_rho0, nch, nseg, d_prog, t0, dt, T, F, h_rw,
-                                         h_tw, d_J, d_grad, st);
+                                         h_tw, dch, npar, d_J, d_grad, st);
         if (rc != SSS_EINVAL || p->batch_variant == 4 || p->batch_variant == 5) return rc;
         set_error("");
     }
     const int N = p->d.N, K = p->d.K, Q = p->d.Q;
-    if (p->d.G < 2) return fail(SSS_EINVAL, "the adjoint needs the x generator (G >= 2)");
+    const int gd = dch + 1;
     BatchLayout Ly;
-    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {1}, false, &Ly, st))
+    if (int rc = build_layout(p, ntraj, d_rho0, nch, nseg, d_prog, dt, F, {gd}, false, &Ly, st))
         return rc;
     SSS_CUDA(cudaMemsetAsync(d_J, 0, sizeof(double) * ntraj, st));
-    SSS_CUDA(cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ntraj * nseg * 2, st));
+    SSS_CUDA(cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ntraj * nseg * npar, st));
     if (Ly.M == 0) return SSS_OK;
     if (Ly.substeps != 1)
         return fail(SSS_EINVAL, "the adjoint needs one sub-step per exponential (use a smaller dt/F)");
     int xg = -1;
     for (int gi = 0; gi < Ly.Ga; gi++)
-        if (Ly.active[gi] == 1) xg = gi;
-    if (xg < 0) return fail(SSS_EINVAL, "the x generator is zero on the reachable rows");
+        if (Ly.active[gi] == gd) xg = gi;
+    if (xg < 0)
+        return fail(SSS_EINVAL, "the generator of channel " + std::to_string(dch) +
+                                    " is zero on the reachable rows");
     const int M = Ly.M, L = Ly.L, E = Ly.E, d = Ly.degree;
     if (d > kAdjMaxTaylor) return fail(SSS_EINVAL, "Taylor degree too large for the adjoint");
     // lane row ranges (lane order) and owner of each row
@@ -1055,6 +1099,7 @@ int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
     AdjArgs a{};
     a.M = M; a.Ga = Ly.Ga; a.K = K; a.Q = Q; a.F = F; a.nch = nch; a.nseg = nseg;
     a.ntraj = ntraj; a.degree = d; a.N = N; a.E = E; a.ET = ET; a.xg = xg;
+    a.dch = dch; a.npar = npar;
     a.n_steps = n_steps; a.T = T; a.C = C; a.n_ck = n_ck;
     a.h = dt / F; a.t0 = t0; a.dt = dt;
     for (int gi = 0; gi < Ly.Ga; gi++) a.gen_index[gi] = Ly.active[gi];

@@ -359,6 +359,7 @@ static int batch_run_impl(sss_plan* p, int ntraj, const double* rho0, int nch, i
             SSS_CUDA(cudaMemcpyAsync(trace, d_tr, sizeof(double) * (size_t)ntraj * T_max * N,
                                      cudaMemcpyDeviceToHost, st));
         SSS_CUDA(cudaStreamSynchronize(st));
+        return batch_check(p, st);
     }
     return SSS_OK;
 }
@@ -379,10 +380,10 @@ int sss_batch_run_table(sss_plan* p, int ntraj, const double* rho0, const double
                           readout_weights, readout, final_state, trace, host, stream);
 }
 
-int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
-                    const double* programs, double t0, double dt, int T, int F,
-                    const double* readout_weights, const double* time_weights, double* J,
-                    double* grad, int host, void* stream) {
+static int adjoint_impl(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                        const double* programs, double t0, double dt, int T, int F,
+                        const double* readout_weights, const double* time_weights, int channel,
+                        int npar, double* J, double* grad, int host, void* stream) {
     if (int rc = check_run(p, ntraj, rho0, nch, nseg, programs, nullptr, dt, T, F,
                            (const void*)J))
         return rc;
@@ -402,7 +403,7 @@ int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nse
         for (size_t i = 0; i < nprog; i++)
             if (std::isnan(programs[i])) return fail(SSS_ENONFINITE, "program contains NaN");
         if (int rc = p->w_in.ensure(sizeof(double) * ((size_t)ntraj * N + nprog))) return rc;
-        if (int rc = p->w_out.ensure(sizeof(double) * ((size_t)ntraj + (size_t)ntraj * nseg * 2)))
+        if (int rc = p->w_out.ensure(sizeof(double) * ((size_t)ntraj + (size_t)ntraj * nseg * npar)))
             return rc;
         double* base = p->w_in.as<double>();
         SSS_CUDA(cudaMemcpyAsync(base, rho0, sizeof(double) * ntraj * N, cudaMemcpyHostToDevice, st));
@@ -414,15 +415,33 @@ int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nse
         d_grad = d_J + ntraj;
     }
     if (int rc = adjoint_run(p, ntraj, d_rho0, nch, nseg, d_prog, t0, dt, T, F, readout_weights,
-                             time_weights, d_J, d_grad, st))
+                             time_weights, channel, npar, d_J, d_grad, st))
         return rc;
     if (host) {
+        const size_t ng = (size_t)ntraj * nseg * npar;
         SSS_CUDA(cudaMemcpyAsync(J, d_J, sizeof(double) * ntraj, cudaMemcpyDeviceToHost, st));
-        SSS_CUDA(cudaMemcpyAsync(grad, d_grad, sizeof(double) * (size_t)ntraj * nseg * 2,
-                                 cudaMemcpyDeviceToHost, st));
+        SSS_CUDA(cudaMemcpyAsync(grad, d_grad, sizeof(double) * ng, cudaMemcpyDeviceToHost, st));
         SSS_CUDA(cudaStreamSynchronize(st));
+        if (!finite_all(J, (size_t)ntraj) || !finite_all(grad, ng))
+            return fail(SSS_ENONFINITE, "adjoint objective or gradient became NaN or Inf");
     }
     return SSS_OK;
+}
+
+int sss_adjoint_run(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                    const double* programs, double t0, double dt, int T, int F,
+                    const double* readout_weights, const double* time_weights, double* J,
+                    double* grad, int host, void* stream) {
+    return adjoint_impl(p, ntraj, rho0, nch, nseg, programs, t0, dt, T, F, readout_weights,
+                        time_weights, 0, 2, J, grad, host, stream);
+}
+
+int sss_adjoint_run_channel(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
+                            const double* programs, double t0, double dt, int T, int F,
+                            const double* readout_weights, const double* time_weights,
+                            int channel, double* J, double* grad, int host, void* stream) {
+    return adjoint_impl(p, ntraj, rho0, nch, nseg, programs, t0, dt, T, F, readout_weights,
+                        time_weights, channel, 4, J, grad, host, stream);
 }
 
 int sss_batch_prepare(sss_plan* p, int ntraj, const double* rho0, int nch, int nseg,
@@ -464,6 +483,11 @@ int sss_batch_launch(sss_plan* p, double* state, const double* programs, const i
         return fail(SSS_EINVAL, "need 0 <= t_begin and t_begin + n_samples <= T_max");
     return batch_launch(p, state, programs, samples, t0, t_begin, n_samples, T_max, readout,
                         (cudaStream_t)stream);
+}
+
+int sss_batch_check(sss_plan* p, void* stream) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    return batch_check(p, (cudaStream_t)stream);
 }
 
 int sss_plan_last_launches(const sss_plan* p) { return p ? p->last_launches : 0; }
@@ -623,7 +647,7 @@ void sss_plan_destroy(sss_plan* p) {
                       &p->w_prop, &p->w_in, &p->w_out, &p->w_prog, &p->w_tab, &p->w_aux,
                       &p->w_queue, &p->w_ro, &p->w_fin, &p->w_samples, &p->w_status,
                       &p->w_state, &p->w_adjf, &p->w_adjb, &p->w_states, &p->w_adjro,
-                      &p->w_adjst, &p->w_order};
+                      &p->w_adjst, &p->w_order, &p->w_health};
     for (DevBuf* b : bufs) b->release();
     for (DevBuf& b : p->batch_tables) b.release();
     if (p->ev_begin) cudaEventDestroy(p->ev_begin);

@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
                     if (ent_end(w)) {
                         int row = ent_end(w) - 1;
                         a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                        note_nonfinite(a, v[row], b, a.t_end);
                     }
                 }
             if (b >= 0 && a.readout)
@@ -254,7 +255,10 @@ __global__ void __launch_bounds__(256) k_batch_lanes(const BatchArgs a) {
                 }
 #pragma unroll
                 for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
-                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+                if (li == 0) {
+                    a.readout[(size_t)b * a.T_max + t] = s;
+                    note_nonfinite(a, s, b, t);
+                }
             }
             t++;
         }
@@ -296,7 +300,10 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
     while (true) {
         if (r == 0 && t >= T_b) {
             if (b >= 0 && a.fin)
-                for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                for (int row = r0; row < r1; row++) {
+                    a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                    note_nonfinite(a, v[row], b, a.t_end);
+                }
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
                     a.readout[(size_t)b * a.T_max + tt] = 0.0;
@@ -380,7 +387,10 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
                 for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
 #pragma unroll
                 for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
-                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+                if (li == 0) {
+                    a.readout[(size_t)b * a.T_max + t] = s;
+                    note_nonfinite(a, s, b, t);
+                }
             }
             t++;
         }
@@ -423,7 +433,10 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
     while (true) {
         if (r == 0 && t >= T_b) {
             if (b >= 0 && a.fin)
-                for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                for (int row = r0; row < r1; row++) {
+                    a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                    note_nonfinite(a, v[row], b, a.t_end);
+                }
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
                     a.readout[(size_t)b * a.T_max + tt] = 0.0;
@@ -503,7 +516,10 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
                 for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
 #pragma unroll
                 for (int o = L / 2; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o);
-                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+                if (li == 0) {
+                    a.readout[(size_t)b * a.T_max + t] = s;
+                    note_nonfinite(a, s, b, t);
+                }
             }
             t++;
         }
@@ -600,7 +616,10 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                 if (a.rot)
                     store_lab(a.fin + (size_t)b * a.N);
                 else
-                    for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                    for (int row = r0; row < r1; row++) {
+                    a.fin[(size_t)b * a.N + a.row_orig[row]] = v[row];
+                    note_nonfinite(a, v[row], b, a.t_end);
+                }
             }
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
@@ -755,7 +774,10 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
                 double s = 0.0;
                 for (int row = r0; row < r1; row++) s = fma(s_rw[row], v[row], s);
                 s = gsum(s);
-                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+                if (li == 0) {
+                    a.readout[(size_t)b * a.T_max + t] = s;
+                    note_nonfinite(a, s, b, t);
+                }
             }
             t++;
         }
@@ -818,7 +840,10 @@ __global__ void __launch_bounds__(256, 1) k_batch_shfl(const BatchArgs a) {
     double v = 0.0;  // this lane's row of the state
     while (true) {
         if (r == 0 && t >= T_b) {
-            if (b >= 0 && a.fin && my_row >= 0) a.fin[(size_t)b * a.N + a.row_orig[my_row]] = v;
+            if (b >= 0 && a.fin && my_row >= 0) {
+                a.fin[(size_t)b * a.N + a.row_orig[my_row]] = v;
+                note_nonfinite(a, v, b, a.t_end);
+            }
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
                     a.readout[(size_t)b * a.T_max + tt] = 0.0;
@@ -904,7 +929,10 @@ __global__ void __launch_bounds__(256, 1) k_batch_shfl(const BatchArgs a) {
                 double s = my_row >= 0 ? s_rw[my_row] * v : 0.0;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
-                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+                if (li == 0) {
+                    a.readout[(size_t)b * a.T_max + t] = s;
+                    note_nonfinite(a, s, b, t);
+                }
             }
             t++;
         }
@@ -2417,8 +2445,24 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
         if (n_next < 0 || p->batch_longest[n_next] <= t) break;
         t = p->batch_longest[n_next];
     }
+    // the health word: all ones while every written value is finite
+    if (int rc = p->w_health.ensure(sizeof(unsigned long long))) return rc;
+    SSS_CUDA(cudaMemsetAsync(p->w_health.p, 0xff, sizeof(unsigned long long), st));
     p->batch_ready = true;
     return SSS_OK;
+}
+
+int batch_check(sss_plan* p, cudaStream_t st) {
+    if (!p->w_health.p) return SSS_OK;
+    unsigned long long h = ~0ull;
+    SSS_CUDA(cudaMemcpyAsync(&h, p->w_health.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+    SSS_CUDA(cudaStreamSynchronize(st));
+    if (h == ~0ull) return SSS_OK;
+    SSS_CUDA(cudaMemsetAsync(p->w_health.p, 0xff, sizeof(h), st));
+    SSS_CUDA(cudaStreamSynchronize(st));
+    return fail(SSS_ENONFINITE, "a state became NaN or Inf: trajectory " +
+                                    std::to_string((unsigned)(h & 0xffffffffu)) +
+                                    ", first at output sample " + std::to_string((unsigned)(h >> 32)));
 }
 
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
@@ -2467,6 +2511,7 @@ int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* 
         a.order = p->batch_order;
         a.tab = d_tab;
         a.rw = d_readout ? a.rw : nullptr;
+        a.health = p->w_health.as<unsigned long long>();
         a.t0 = t0;
         a.t_begin = t;
         a.t_end = stop;

@@ -73,7 +73,19 @@ struct BatchArgs {
     unsigned amask[kMaxSlots]; // per live generator: slots with a non-zero value in some lane
     double cfac[kMaxTaylor + 1];  // scaled Horner: c_j = d!/(j-1)!
     double inv_dfact;          // 1/d!
+    // health word of the run, or null: all ones while every readout and
+    // final-state entry written so far is finite, else the smallest
+    // (output sample << 32 | trajectory) that was not
+    unsigned long long* health;
 };
+
+// Records a non-finite readout or final-state entry x of trajectory b at
+// output sample t (a final state counts as sample t_end) in the health word.
+// One compare per written value; the atomic runs only on the error path.
+__device__ __forceinline__ void note_nonfinite(const BatchArgs& a, double x, int b, int t) {
+    if (!isfinite(x) && a.health)
+        atomicMin(a.health, ((unsigned long long)(unsigned)t << 32) | (unsigned)b);
+}
 
 // Slot words.
 // Logical words (the packer's, and sss_slot_layout's): bits 0-13 the row an

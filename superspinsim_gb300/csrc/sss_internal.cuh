@@ -105,6 +105,9 @@ struct sss_plan {
     // workspace
     sss::DevBuf w_prop, w_in, w_out, w_prog, w_tab, w_aux, w_queue, w_ro,
         w_fin, w_samples, w_status;
+    // health word of the prepared batch (see BatchArgs::health), reset by
+    // sss_batch_prepare and by a check that found an error
+    sss::DevBuf w_health;
     int last_launches = 0;
     int batch_lanes = 0;    // 0: chosen per run
     int batch_threads = 0;  // CTA size of the batched kernel, 0: 128
@@ -174,9 +177,12 @@ int batch_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
               const double* d_tab = nullptr);
 int build_sparse(sss_plan* p);
 // sss_adjoint.cu
+// dch: the differentiated channel; npar: 2 (amplitude, phase) or 4 (also
+// offset, frequency) gradient entries per segment
 int adjoint_run(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                 const double* d_prog, double t0, double dt, int T, int F, const double* h_rw,
-                const double* h_tw, double* d_J, double* d_grad, cudaStream_t st);
+                const double* h_tw, int dch, int npar, double* d_J, double* d_grad,
+                cudaStream_t st);
 // d_tab: a coefficient table (ntraj*(F*T_tab*Q)*G, rows (r*T_tab + t)*Q + k)
 // in place of the programs; it runs on the row-part kernel
 // h_samples: the trajectories' output-sample counts (host), or null; with
@@ -188,6 +194,10 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
 int batch_launch(sss_plan* p, double* d_state, const double* d_prog, const int* d_samples,
                  double t0, int t_begin, int n_samples, int T_max, double* d_readout,
                  cudaStream_t st, double* d_trace = nullptr, const double* d_tab = nullptr);
+// Waits for the stream and reads the prepared batch's health word:
+// SSS_ENONFINITE (and the word reset) if a launch since the last prepare or
+// check wrote a NaN or infinite readout or final-state entry.
+int batch_check(sss_plan* p, cudaStream_t st);
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                  const double* d_prog, double dt, int F, const std::vector<int>& force_active,
                  bool allow_register, BatchLayout* out, cudaStream_t st, bool force_parts = false,

@@ -255,7 +255,10 @@ __global__ void __launch_bounds__(256, 1) k_batch_slots(const BatchArgs a) {
                 if (a.rot)
                     store_lab(a.fin + (size_t)b * a.N);
                 else
-                    for (int row = r0; row < r1; row++) a.fin[(size_t)b * a.N + a.row_orig[row]] = V[row];
+                    for (int row = r0; row < r1; row++) {
+                    a.fin[(size_t)b * a.N + a.row_orig[row]] = V[row];
+                    note_nonfinite(a, V[row], b, a.t_end);
+                }
             }
             if (b >= 0 && a.readout)
                 for (int tt = max(T_b, a.t_begin) + li; tt < a.t_end; tt += L)
@@ -389,7 +392,10 @@ __global__ void __launch_bounds__(256, 1) k_batch_slots(const BatchArgs a) {
                 double s = 0.0;
                 for (int row = r0; row < r1; row++) s = fma(s_rw[row], V[row], s);
                 s = gsum(s);
-                if (li == 0) a.readout[(size_t)b * a.T_max + t] = s;
+                if (li == 0) {
+                    a.readout[(size_t)b * a.T_max + t] = s;
+                    note_nonfinite(a, s, b, t);
+                }
             }
             t++;
         }

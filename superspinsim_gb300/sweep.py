@@ -224,7 +224,11 @@ class ChunkedRun:
             self.t_next += n
         return self.t_next
 
-    def run(self, chunk):
+    def run(self, chunk=None):
+        """Run the remaining samples in launches of `chunk` output samples
+        (default: the autotuner's launch length for this sweep, else all
+        remaining samples in one launch)."""
+        chunk = chunk or getattr(self.sweep, "tuned_chunk", None) or self.T_max
         while self.t_next < self.T_max:
             self.step(chunk)
         return self
@@ -278,7 +282,14 @@ class ChunkedRun:
                 self.readout.copy_(self.torch.from_numpy(z["readout"]))
         return self
 
+    def check(self):
+        """Raise SSSError (ENONFINITE) if a chunk so far wrote a NaN or
+        infinite readout or final state (waits for the current stream)."""
+        self.sweep.plan.batch_check(self.torch.cuda.current_stream().cuda_stream)
+        return self
+
     def results(self):
+        self.check()
         out = {"final": self.state.cpu().numpy()}
         if self.readout is not None:
             out["readout"] = self.readout.cpu().numpy()

@@ -3,9 +3,13 @@
 Times short prepared launches of the actual batch (a few output samples of
 every trajectory) for each candidate configuration -- lanes per trajectory,
 kernel variant (two FMA chains per row, one, row parts, packed slots or
-phased row parts) and CTA size -- with CUDA
-events on the launch stream, keeps the fastest, and caches the choice per
-(model, batch size, fine steps) for the process.
+phased row parts) and CTA size -- with CUDA events on the launch stream,
+keeps the fastest, and then, for that configuration, times a window of
+output samples run as launches of each candidate length (steps per launch,
+in output samples of F fine steps): short launches give finer resume
+points and graph chunks, long ones amortise the launch and the tail of
+each launch.  The choice is cached per (model, batch size, fine steps) for
+the process.
 """
 import itertools
 
@@ -25,10 +29,14 @@ def _key(sweep, B, progs):
 
 def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, repeats=2,
              lanes=(0, 8, 16, 32, 64, 128), variants=(1, 3, 4, 6, 7), threads=(32, 64, 128),
-             use_cache=True):
-    """Pick and set the fastest batch configuration for this sweep and batch.
-    Returns {"config": (lanes, variant, threads), "ms_per_traj_step": ...,
-    "trials": [...]}."""
+             chunks=(1, 4, 16, 64), chunk_tolerance=0.01, use_cache=True):
+    """Pick and set the fastest batch configuration for this sweep and batch,
+    then its launch length.  Returns {"config": (lanes, variant, threads),
+    "ms_per_traj_step": ..., "trials": [...], "samples_per_launch": c,
+    "chunk_trials": [...]}: c is the shortest candidate launch length (in
+    output samples) whose time over a window of max(chunks) samples is
+    within chunk_tolerance of the best (chunks=() skips this stage; c is
+    then None).  ChunkedRun.run uses it when given no chunk length."""
     import torch
     progs = stack(programs) if isinstance(programs, (list, tuple)) and programs and \
         isinstance(programs[0], Program) else np.ascontiguousarray(programs, dtype=np.float64)
@@ -41,6 +49,7 @@ def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, re
         best = _CACHE[key]
         L, var, th = best["config"]
         sweep.plan.set_batch_config(lanes=L, cta_threads=th, variant=var)
+        sweep.tuned_chunk = best["samples_per_launch"]
         return best
     dev = torch.device("cuda")
     d_rho0 = torch.from_numpy(np.ascontiguousarray(flat)).to(dev)
@@ -80,8 +89,35 @@ def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, re
         raise RuntimeError("no batch configuration fits: " + str(trials))
     best = min(ok, key=lambda t: t["ms"])
     steps = B*probe_samples*sweep.F
-    result = {"config": best["config"], "ms_per_traj_step": best["ms"]/steps, "trials": trials}
+    result = {"config": best["config"], "ms_per_traj_step": best["ms"]/steps, "trials": trials,
+              "samples_per_launch": None, "chunk_trials": []}
     L, var, th = best["config"]
     sweep.plan.set_batch_config(lanes=L, cta_threads=th, variant=var)
+    if chunks:
+        sweep.plan.batch_prepare(d_rho0.data_ptr(), B, d_prog.data_ptr(), progs.shape[1],
+                                 progs.shape[2], time_step, sweep.F, stream=stream.cuda_stream)
+        window = max(chunks)
+        for c in sorted(chunks):
+            times = []
+            for _ in range(repeats):
+                state.copy_(d_rho0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for t in range(0, window, c):
+                    sweep.plan.batch_launch(state.data_ptr(), d_prog.data_ptr(), 0.0, t,
+                                            min(c, window - t), window,
+                                            stream=stream.cuda_stream)
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            result["chunk_trials"].append({"samples_per_launch": c, "launches": -(-window//c),
+                                           "ms": min(times),
+                                           "ms_per_traj_step": min(times)/(B*window*sweep.F)})
+        fastest = min(t["ms"] for t in result["chunk_trials"])
+        result["samples_per_launch"] = min(
+            t["samples_per_launch"] for t in result["chunk_trials"]
+            if t["ms"] <= fastest*(1 + chunk_tolerance))
+    sweep.tuned_chunk = result["samples_per_launch"]
     _CACHE[key] = result
     return result

@@ -80,6 +80,79 @@ def test_adjoint_objective_matches_forward_and_fd(variant):
         assert abs(grad[b, s, comp] - fd) <= 1e-5*abs(fd) + 1e-13*abs(J[b])/hh
 
 
+def _two_channel_problem():
+    """Pulse shapes on x plus a y drive (half the amplitude, other phases,
+    detuned by 2 MHz) on channel 1; the laser on channel 3 is off during
+    the pulses and on for the readout."""
+    rabi, phase, progs, dur = _problem(seed=11, B=2, S=3)
+    progs[:, 1] = progs[:, 0]
+    progs[:, 1, :3, 2] *= 0.5
+    progs[:, 1, :3, 3] += 2e6
+    progs[:, 1, :3, 4] += 0.7
+    return progs, dur
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("channel", [0, 1, 3])
+def test_channel_adjoint_matches_fd(channel, variant):
+    """sss_adjoint_run_channel: d J / d (amplitude, phase, offset, frequency)
+    of the segments of the x drive, of a detuned y drive and of the laser,
+    against Richardson-extrapolated central differences of the GPU forward.
+    On channel 0 its first two entries equal sss_adjoint_run's bit for bit."""
+    from superspinsim_gb300.adjoint import trapezoid_weights
+    obj, c, rho = _objective()
+    obj.plan.set_batch_config(variant=variant)
+    progs, dur = _two_channel_problem()
+    dt = 1e-9
+    T = int(round(dur[0]/dt))
+    tw = trapezoid_weights(T, dt, 5, T - 1)
+    J, g4 = obj.run(progs, dt, T, tw, channel=channel)
+    assert g4.shape == progs.shape[:1] + (progs.shape[2], 4)
+    Jf = obj.forward_only(progs, dt, T, tw)
+    assert np.abs(J - Jf).max() <= 1e-12*np.abs(Jf).max()
+    if channel == 0:
+        J2, g2 = obj.run(progs, dt, T, tw)
+        assert np.array_equal(J2, J) and np.array_equal(g2, g4[..., :2])
+    # (program column, step) per parameter: amplitude, phase, offset, frequency
+    B, S = progs.shape[0], progs.shape[2]
+    pert, idx = [], []
+    for b in range(B):
+        for s in range(S):
+            seg = progs[b, channel, s]
+            amp_h = 1e-3*max(abs(seg[2]), abs(seg[1]), 1e-3)
+            for comp, col, h in ((0, 2, amp_h), (1, 4, 1e-3), (2, 1, amp_h), (3, 3, 1e4)):
+                for step in (h, -h, 2*h, -2*h):
+                    p = progs[b].copy()
+                    p[channel, s, col] += step
+                    pert.append(p)
+                idx.append((b, s, comp, h))
+    Jp = obj.forward_only(np.stack(pert), dt, T, tw)
+    scale = np.abs(g4).max()
+    for k, (b, s, comp, h) in enumerate(idx):
+        d1 = (Jp[4*k] - Jp[4*k + 1])/(2*h)
+        d2 = (Jp[4*k + 2] - Jp[4*k + 3])/(4*h)
+        fd = (4*d1 - d2)/3
+        atol = 1e-11*abs(J[b])/h + 1e-9*scale
+        assert abs(g4[b, s, comp] - fd) <= 1e-6*abs(fd) + atol, \
+            (b, s, comp, g4[b, s, comp], fd)
+    if channel == 3:
+        # a constant segment: d/d amplitude = d/d offset, phase and frequency 0
+        assert np.array_equal(g4[..., 0], g4[..., 2])
+        assert not g4[..., 1].any() and not g4[..., 3].any()
+
+
+def test_channel_adjoint_rejects_a_channel_without_generator():
+    from superspinsim_gb300 import _lib
+    from superspinsim_gb300.adjoint import trapezoid_weights
+    obj, c, rho = _objective()
+    progs, dur = _two_channel_problem()
+    T = int(round(dur[0]/1e-9))
+    tw = trapezoid_weights(T, 1e-9, 5, T - 1)
+    with pytest.raises(_lib.SSSError) as e:
+        obj.run(progs, 1e-9, T, tw, channel=4)
+    assert e.value.code == -1
+
+
 def test_adjoint_matches_fd_of_oracle():
     """Finite differences of the CPU oracle in reference mode (the
     reference's own algorithm: 4^-35 scaling and 70 residual squarings per

@@ -230,6 +230,43 @@ def test_chunked_runs_graph_replay_and_resume(tmp_path, variant):
     assert np.array_equal(r3["final"], one["final"])
 
 
+@pytest.mark.parametrize("name", ["coherent_chain", "hbn_bell"])
+@pytest.mark.parametrize("variant", [0, 4, 7])
+def test_batch_coupled_blocks_against_oracle(name, variant):
+    """Systems with coherent block couplings (Vc in L0, Vr in Gr, scaled by
+    the fourth channel) and with Bell-state couplings through the batched
+    kernel: a sweep over the drive frequency and the fourth channel's
+    level, final states and readouts against the oracle."""
+    from superspinsim_gb300 import _lib
+    from superspinsim_gb300.quadratures import method
+    c = load_case(name)
+    vm = c["vectorisation_map"]
+    N = vm.shape[0]
+    B = 8
+    progs = np.repeat(c["program"][None], B, axis=0)
+    progs[:, 0, 0, 3] *= np.linspace(0.9, 1.1, B)
+    progs[:, 3, 0, 0] = 1.0
+    progs[:, 3, 0, 1] = np.linspace(0.0, 1.0, B)
+    rho0 = np.stack([oracle.flatten(c["rho0"], vm, N)]*B)
+    w = np.array([1.0 if y == x and ch == 0 else 0.0 for y, x, ch in vm])
+    w[0] = 2.0
+    W, nodes = method(2)
+    T, dt, F = 4, 1e-9, 20
+    plan = _lib.Plan(c["generators"], W, nodes)
+    plan.set_batch_config(variant=variant)
+    ro, fin = plan.batch(rho0, progs, 0.0, dt, T, F, readout_weights=w, want_final=True)
+    _, ref = oracle.simulate(c["generators"], np.stack([c["rho0"]]*B), 0.0, T*dt + 1e-13, dt,
+                             progs, K=2, W=W, nodes=nodes, F=F, vectorisation_map=vm,
+                             mode="vector", degree=16, flat_out=True)
+    assert np.abs(fin - ref[:, -1]).max() <= 1e-12
+    assert np.abs(ro - ref @ w).max() <= 1e-12
+    if name == "coherent_chain":
+        # the second qubit (levels 5, 6) is reached only through the Vr
+        # coupling: empty at level 0 of the fourth channel, filled at 1
+        q2 = [k for k, (y, x, ch) in enumerate(vm) if y == x and y in (5, 6) and ch == 0]
+        assert np.abs(fin[0, q2]).max() <= 1e-15 and fin[-1, q2].sum() > 1e-4
+
+
 def test_autotuner_picks_a_working_configuration():
     pytest.importorskip("torch")
     from superspinsim_gb300 import protocols
@@ -248,6 +285,37 @@ def test_autotuner_picks_a_working_configuration():
     sw2 = Sweep(c["generators"], vm, number_of_exponentials=2, number_of_fine_divisions=20)
     out2 = sw2.run(rho, progs, 0.0, 3e-9 + 1e-13, 1e-9, readout_weights=w, final_state=True)
     assert np.abs(out["final"] - out2["final"]).max() <= 1e-13
+
+
+def test_autotuner_times_launch_lengths():
+    """The launch-length stage times a 16-sample window as 16, 4 and 1
+    launches for the chosen configuration, picks the shortest launch within
+    the tolerance of the fastest, and a ChunkedRun with no chunk length
+    uses it; the chunked result equals a single launch bit for bit."""
+    pytest.importorskip("torch")
+    from superspinsim_gb300 import protocols
+    from superspinsim_gb300.sweep import ChunkedRun, Sweep, population_weights
+    from superspinsim_gb300.tune import autotune
+    c = load_case("nv7_n49")
+    vm = c["vectorisation_map"]
+    progs = protocols.odmr(2.870e9 + 28.025e9*5e-3 + np.linspace(-5e6, 5e6, 40), 5e6, 0.15)
+    rho = np.zeros((7, 7), complex)
+    rho[1, 1] = 1
+    sw = Sweep(c["generators"], vm, number_of_exponentials=2, number_of_fine_divisions=10)
+    res = autotune(sw, rho, progs, 1e-9, probe_samples=1, repeats=1, lanes=(0, 32),
+                   variants=(4, 7), threads=(32,), chunks=(1, 4, 16), use_cache=False)
+    trials = res["chunk_trials"]
+    assert [t["launches"] for t in trials] == [16, 4, 1]
+    best = min(t["ms"] for t in trials)
+    c_pick = res["samples_per_launch"]
+    assert c_pick in (1, 4, 16) and sw.tuned_chunk == c_pick
+    assert next(t for t in trials if t["samples_per_launch"] == c_pick)["ms"] <= best*1.01
+    w = population_weights(vm, [3, 4, 5])
+    T = 12
+    tuned = ChunkedRun(sw, rho, progs, 0.0, 1e-9, T, readout_weights=w).run().results()
+    whole = ChunkedRun(sw, rho, progs, 0.0, 1e-9, T, readout_weights=w).run(chunk=T).results()
+    assert np.array_equal(tuned["readout"], whole["readout"])
+    assert np.array_equal(tuned["final"], whole["final"])
 
 
 def test_dropin_simulate_nv21_uses_batched_trace():
