@@ -626,7 +626,7 @@ def main():
                            "trials": len(tuned["trials"]),
                            "samples_per_launch": tuned["samples_per_launch"],
                            "launch_length_trials": {
-                               str(t["samples_per_launch"]): round(t["ms_per_traj_step"]*1e9, 4)
+                               str(t["samples_per_launch"]): round(t["ms_per_traj_step"]*1e6, 5)
                                for t in tuned["chunk_trials"]},
                            "launch_length_unit": "ns per traj-step over a 64-sample window"},
                        "kernel": {"lanes": info["lanes"], "taylor_degree": info["degree"],
@@ -635,6 +635,8 @@ def main():
                                   "live_generators": info["live_generators"],
                                   "live_nnz": info["live_nnz"],
                                   "fp64_per_horner_term": info["fp64_per_term"],
+                                  "bank_extra_wavefronts_per_term":
+                                      info["bank_extra_wavefronts_per_term"],
                                   # uneven lengths run in phases of widening lane
                                   # groups; "lanes" is the last phase's
                                   "launches_per_run": n_chunks or plan.last_launches()},

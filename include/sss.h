@@ -357,6 +357,15 @@ int sss_slot_layout(int M, const int* row_ptr, const int* col, int lanes,
  * (those whose coefficient varies; the constant ones are folded into a
  * table), their non-zeros on the pruned pattern, and the FP64 instructions
  * one group issues per Horner term.  Any pointer may be NULL. */
+/* Shared-memory bank conflicts of the last slot-programmed layout (variants
+ * 6 and 7; no reference counterpart): the extra wavefronts one Horner term
+ * of one group costs, as modelled on the host from the layout's loads and
+ * stores (per half-warp and instruction, the distinct 8-byte words beyond
+ * one per bank), with the rows numbered in lane order (before) and after
+ * the bank-aware renumbering the layout runs with (after).  Any pointer
+ * may be NULL. */
+int sss_plan_bank_conflicts(const sss_plan* plan, int* before, int* after);
+
 int sss_plan_batch_work(const sss_plan* plan, int* variant, int* live_generators,
                         int* live_nnz, int* fp64_per_term);
 

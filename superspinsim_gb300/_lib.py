@@ -26,7 +26,7 @@ SYMBOLS = ["sss_plan_create", "sss_plan_set_rotating", "sss_simulate",
            "sss_plan_set_batch_config", "sss_plan_batch_info", "sss_plan_set_adjoint_memory",
            "sss_plan_set_projection", "sss_plan_set_unitary",
            "sss_fp64_peak", "sss_fp64_mma_peak", "sss_simulate_noalloc", "sss_adjoint_run", "sss_adjoint_run_channel", "sss_batch_prepare",
-           "sss_batch_prepare_samples", "sss_batch_launch", "sss_batch_check", "sss_slot_layout", "sss_plan_batch_work", "sss_last_error",
+           "sss_batch_prepare_samples", "sss_batch_launch", "sss_batch_check", "sss_slot_layout", "sss_plan_batch_work", "sss_plan_bank_conflicts", "sss_last_error",
            "sss_plan_destroy"]
 
 
@@ -105,6 +105,8 @@ def load(build_if_missing=True):
         L.sss_slot_layout.restype = i
         L.sss_plan_batch_work.argtypes = [vp, ip, ip, ip, ip]
         L.sss_plan_batch_work.restype = i
+        L.sss_plan_bank_conflicts.argtypes = [vp, ip, ip]
+        L.sss_plan_bank_conflicts.restype = i
         L.sss_last_error.restype = ctypes.c_char_p
         L.sss_plan_destroy.argtypes = [vp]
         L.sss_plan_destroy.restype = None
@@ -371,6 +373,10 @@ class Plan:
         check(load().sss_plan_batch_work(self._h, *[ctypes.byref(v) for v in work]))
         out.update(zip(["variant", "live_generators", "live_nnz", "fp64_per_term"],
                        [v.value for v in work]))
+        bank = [ctypes.c_int() for _ in range(2)]
+        check(load().sss_plan_bank_conflicts(self._h, *[ctypes.byref(v) for v in bank]))
+        out["bank_extra_wavefronts_per_term"] = {"lane_order": bank[0].value,
+                                                 "renumbered": bank[1].value}
         return out
 
     def last_launches(self):

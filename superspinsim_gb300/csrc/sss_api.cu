@@ -620,6 +620,13 @@ int sss_plan_batch_work(const sss_plan* p, int* variant, int* live_generators, i
     return SSS_OK;
 }
 
+int sss_plan_bank_conflicts(const sss_plan* p, int* before, int* after) {
+    if (!p) return fail(SSS_EINVAL, "null plan");
+    if (before) *before = p->last_bank_before;
+    if (after) *after = p->last_bank_after;
+    return SSS_OK;
+}
+
 int sss_plan_batch_info(const sss_plan* p, int* lanes, int* degree, int* substeps, int* rows,
                         int* nnz, double* kernel_ms) {
     if (!p) return fail(SSS_EINVAL, "null plan");

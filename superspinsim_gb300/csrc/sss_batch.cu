@@ -46,6 +46,7 @@
 #include <random>
 #include <vector>
 
+#include "sss_banks.h"
 #include "sss_batch_args.cuh"
 #include "sss_device.cuh"
 #include "sss_internal.cuh"
@@ -1503,6 +1504,191 @@ static int emit_slot_cells(sss_plan* p, const std::vector<std::vector<BatchLayou
     return SSS_OK;
 }
 
+// Places the rows, parked partial sums and piece items of a slot-programmed
+// layout for few shared-memory bank conflicts (optimise_banks) and pads the
+// buffer stride M + 2 + npart to a multiple of 16 words, so that word i of
+// V, A and B falls in the same bank.  The accesses of one Horner term:
+// every slot's operand load, the reloads of parked partial sums after the
+// barrier, the loads of phase-2 start values and every store.  Items move
+// only inside their piece (or chain) and only among their kind: entries
+// of generators assembled every exponential (varies[g]) among themselves,
+// so the assembly touches the same slots; other entries and v terms among
+// themselves; partial adds stay (they must follow the barrier).  Rewrites
+// the kernel words, entry indices, generator values, newpos, row_orig and
+// the lanes' row ranges (an even split: the kernels' per-row loops sit
+// between group barriers, so any partition of the rows serves).
+static int bank_relabel(sss_plan* p, BatchLayout& Ly, const std::vector<int>& active,
+                        const std::vector<char>& varies) {
+    const int L = Ly.L, S = Ly.S, M = Ly.M, np = Ly.npart, Ga = (int)active.size();
+    const int sink = M + 1, n_items = M + 2 + np, bar = Ly.bar_at;
+    std::vector<unsigned>& cw = Ly.cw;
+    auto ldw = [&](int q, int l) { return cw[(size_t)q * L + l]; };
+    auto stw = [&](int q, int l) { return cw[(size_t)(S + q) * L + l]; };
+    BankProblem pb;
+    pb.L = L;
+    auto buf_of = [](unsigned w) {
+        const unsigned src = w & (3u << 14);
+        return src == kLdV ? 0 : (src == kLdNext ? 2 : 1);
+    };
+    // instructions: the S operand loads first (cell q*L + l), then the
+    // reloads of partial sums after the barrier, start-value loads and stores
+    auto instr = [&](auto fn) {  // fn(l) -> access
+        for (int l = 0; l < L; l++) pb.cell.push_back(fn(l));
+        pb.n_instr++;
+    };
+    for (int q = 0; q < S; q++)
+        instr([&, q](int l) { return BankAccess{buf_of(ldw(q, l)), (int)(ldw(q, l) & kSlotIdx)}; });
+    for (int q = bar; q < S; q++)
+        instr([&, q](int l) {
+            const unsigned w = ldw(q, l);
+            return (w & (3u << 14)) == kLdNext ? BankAccess{2, (int)(w & kSlotIdx)} : BankAccess{-1, 0};
+        });
+    auto add_store = [&](int q) {
+        instr([&, q](int l) {
+            const int st = (int)(stw(q, l) & kSlotIdx);
+            return st == sink ? BankAccess{-1, 0} : BankAccess{2, st};
+        });
+    };
+    auto add_base = [&](int q) {
+        instr([&, q](int l) { return BankAccess{2, (int)((stw(q, l) >> 14) & kSlotIdx)}; });
+    };
+    // pieces (slot-packed: from a start slot to a storing slot) or chains
+    // (phased), as lists of load cells per lane
+    std::vector<std::vector<int>> pieces;
+    if (Ly.phased) {
+        const PhasedShape& sh = kPhasedShapes[Ly.shape];
+        const int S1 = sh.C1 * sh.P1;
+        for (int c = 0; c < sh.C1; c++) add_store((sh.P1 - 1) * sh.C1 + c);
+        for (int c = 0; c < sh.C2; c++) {
+            add_base(S1 + c);
+            add_store(S1 + (sh.P2 - 1) * sh.C2 + c);
+        }
+        for (int l = 0; l < L; l++) {
+            for (int c = 0; c < sh.C1; c++) {
+                pieces.emplace_back();
+                for (int e = 0; e < sh.P1; e++) pieces.back().push_back((e * sh.C1 + c) * L + l);
+            }
+            for (int c = 0; c < sh.C2; c++) {
+                pieces.emplace_back();
+                for (int e = 0; e < sh.P2; e++) pieces.back().push_back((S1 + e * sh.C2 + c) * L + l);
+            }
+        }
+    } else {
+        for (int q = 0; q < S; q++) {
+            add_store(q);
+            if (q >= bar) add_base(q);
+        }
+        for (int l = 0; l < L; l++) {
+            std::vector<int> cur;
+            for (int q = 0; q < S; q++) {
+                if ((stw(q, l) & kStStart) && !cur.empty()) {
+                    pieces.push_back(cur);
+                    cur.clear();
+                }
+                cur.push_back(q * L + l);
+                if ((int)(stw(q, l) & kSlotIdx) != sink) {
+                    pieces.push_back(cur);
+                    cur.clear();
+                }
+            }
+            if (!cur.empty()) pieces.push_back(cur);
+        }
+    }
+    for (const auto& pc : pieces) {
+        std::vector<int> var, other;
+        for (int c : pc) {
+            const int q = c / L, l = c % L;
+            const unsigned w = ldw(q, l);
+            if ((w & (3u << 14)) == kLdNext) continue;  // partial adds stay
+            bool v = false;
+            for (int gi = 0; gi < Ga && !v; gi++)
+                v = active[gi] < (int)varies.size() && varies[active[gi]] &&
+                    Ly.gv[((size_t)gi * S + q) * L + l] != 0.0;
+            (v ? var : other).push_back(c);
+        }
+        if (var.size() >= 2) pb.cell_sets.push_back(var);
+        if (other.size() >= 2) pb.cell_sets.push_back(other);
+    }
+    for (const BankAccess& a : pb.cell)
+        if (a.buf >= 0 && (a.item < 0 || a.item >= n_items))
+            return fail(SSS_EINVAL, "slot word out of range");
+    pb.classes.resize(2);
+    for (int i = 0; i < M; i++) pb.classes[0].push_back(i);
+    for (int i = M + 2; i < n_items; i++) pb.classes[1].push_back(i);
+    // cached per layout (FNV-1a over the kernel words and the item kinds)
+    uint64_t key = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { key = (key ^ v) * 1099511628211ull; };
+    for (uint64_t v : {(uint64_t)L, (uint64_t)S, (uint64_t)M, (uint64_t)np, (uint64_t)Ly.phased,
+                       (uint64_t)Ly.shape, (uint64_t)bar})
+        mix(v);
+    for (unsigned w : cw) mix(w);
+    for (const auto& cs : pb.cell_sets) {
+        mix(0xffffffffull);
+        for (int c : cs) mix((uint64_t)c);
+    }
+    std::vector<int> pos(n_items), origin;
+    for (int i = 0; i < n_items; i++) pos[i] = i;
+    int before = 0, after = 0;
+    const int n_load = S * L;
+    auto hit = p->bank_cache.find(key);
+    if (hit != p->bank_cache.end() && (int)hit->second.size() == n_items + n_load) {
+        before = bank_total_cost(pb, pos);
+        pos.assign(hit->second.begin(), hit->second.begin() + n_items);
+        origin.assign(hit->second.begin() + n_items, hit->second.end());
+        std::vector<BankAccess> moved(pb.cell);
+        for (int c = 0; c < n_load; c++) moved[c] = pb.cell[origin[c]];
+        pb.cell = moved;
+        after = bank_total_cost(pb, pos);
+    } else {
+        const long budget = std::min<long>(8000000L, 300000L + 6000L * (long)(M + np));
+        after = optimise_banks(pb, pos, origin, budget, &before);
+        origin.resize(n_load);
+        std::vector<int> entry(pos);
+        entry.insert(entry.end(), origin.begin(), origin.end());
+        p->bank_cache[key] = entry;
+    }
+    p->last_bank_before = before;
+    p->last_bank_after = after;
+    // rewrite: items moved within lanes (load words, entry indices,
+    // generator values), then every word relabelled
+    {
+        const std::vector<unsigned> cw0(cw);
+        const std::vector<int> eq0(Ly.entry_q);
+        const std::vector<double> gv0(Ly.gv);
+        for (int c = 0; c < n_load; c++) {
+            const int o = origin[c];
+            if (o == c) continue;
+            const int q = c / L, l = c % L, qo = o / L;
+            cw[(size_t)q * L + l] = cw0[(size_t)qo * L + l];
+            Ly.entry_q[(size_t)q * L + l] = eq0[(size_t)qo * L + l];
+            for (int gi = 0; gi < Ga; gi++)
+                Ly.gv[((size_t)gi * S + q) * L + l] = gv0[((size_t)gi * S + qo) * L + l];
+        }
+    }
+    for (int q = 0; q < S; q++)
+        for (int l = 0; l < L; l++) {
+            unsigned& w = cw[(size_t)q * L + l];
+            w = (w & ~kSlotIdx) | (unsigned)pos[w & kSlotIdx];
+            unsigned& s2 = cw[(size_t)(S + q) * L + l];
+            const unsigned st = s2 & kSlotIdx, base = (s2 >> 14) & kSlotIdx;
+            s2 = (s2 & ~(kSlotIdx | (kSlotIdx << 14))) | (unsigned)pos[st] |
+                 ((unsigned)pos[base] << 14);
+        }
+    std::vector<int> row_orig(M), inv(M);
+    for (int k = 0; k < M; k++) row_orig[pos[k]] = Ly.row_orig[k];
+    Ly.row_orig = row_orig;
+    for (int& r : Ly.newpos)
+        if (r >= 0) r = pos[r];
+    for (int i = 0; i < (int)Ly.newpos.size(); i++)
+        if (Ly.newpos[i] >= 0) inv[Ly.newpos[i]] = i;
+    Ly.lane_of.assign(L, {});
+    for (int l = 0; l < L; l++)
+        for (int k = (int)((long)M * l / L); k < (int)((long)M * (l + 1) / L); k++)
+            Ly.lane_of[l].push_back(inv[k]);
+    Ly.npart = (M + 2 + np + 15) / 16 * 16 - (M + 2);
+    return SSS_OK;
+}
+
 static void set_slot_fields(BatchLayout& Ly, int L, int S, int SA, int npart, int threads) {
     Ly.parts = true;
     Ly.slots = true;
@@ -1970,7 +2156,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
             chosen = auto_lanes(p, p->auto_cost, n_rule);
         }
         if (chosen && best_at(chosen, true) > 0.0) {
-            rc = SSS_OK;
+            rc = Ly.slots ? bank_relabel(p, Ly, active, varies) : SSS_OK;
         } else {
             const char* what = slots_asked ? "slot-packed" : phased_asked ? "phased row-part" : "row-part";
             rc = chosen ? fail(SSS_EINVAL, std::string(what) + " variant does not fit this pattern at " +

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "sss.h"
@@ -117,6 +118,12 @@ struct sss_plan {
     // per exponential, their non-zeros on the pruned pattern, FP64
     // instructions per Horner term per group; make_args records the first two
     int last_n_live = 0, last_live_nnz = 0, last_fp64_per_term = 0, mk_n_live = 0, mk_live_nnz = 0;
+    // bank-aware renumbering of slot-programmed layouts: the modelled extra
+    // shared-memory wavefronts of one Horner term (one group) before and
+    // after, for the last layout built, and the numberings found so far
+    // (keyed by a hash of the layout's kernel words)
+    int last_bank_before = 0, last_bank_after = 0;
+    std::unordered_map<uint64_t, std::vector<int>> bank_cache;
     int batch_variant = 0;  // 0: register variant when it fits, 2: shared-memory variant,
                             // 3: one-chain register variant, 4: row-part variant
     int device = 0;
