@@ -1640,7 +1640,8 @@ static int bank_relabel(sss_plan* p, BatchLayout& Ly, const std::vector<int>& ac
         pb.cell = moved;
         after = bank_total_cost(pb, pos);
     } else {
-        const long budget = std::min<long>(8000000L, 300000L + 6000L * (long)(M + np));
+        // about 0.1 s of host time for NV-7 (26 labels), 1 s for NV-21 (249)
+        const long budget = std::min<long>(6000000L, 300000L + 20000L * (long)(M + np));
         after = optimise_banks(pb, pos, origin, budget, &before);
         origin.resize(n_load);
         std::vector<int> entry(pos);
