@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                 for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
                 for (int gi = 0; gi < NL; gi++) {
                     const double c = ring_ag[(rp * K + e_exp) * NL + gi];
-                    if (c == 0.0) continue;
+                    if (is_zero(c)) continue;
                     const double* gv = a.gv + (size_t)a.live[gi] * CP * L + li;
 #pragma unroll
                     for (int e = 0; e < CP; e++) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);

@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(256) k_batch_reg(const BatchArgs a) {
             for (int e = 0; e < EPL; e++) om[e] = 0.0;
             for (int g = 0; g < Ga; g++) {
                 const double c = ag[g];
-                if (c == 0.0) continue;
+                if (is_zero(c)) continue;
                 const double* gv = a.gv + (size_t)g * EPL * L + li;
 #pragma unroll
                 for (int e = 0; e < EPL; e++)
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(256) k_batch_reg1(const BatchArgs a) {
             for (int e = 0; e < EPL; e++) om[e] = 0.0;
             for (int g = 0; g < Ga; g++) {
                 const double c = ag[g];
-                if (c == 0.0) continue;
+                if (is_zero(c)) continue;
                 const double* gv = a.gv + (size_t)g * EPL * L + li;
 #pragma unroll
                 for (int e = 0; e < EPL; e++)
@@ -708,7 +708,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_parts(const BatchArgs a) {
             for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
             for (int gi = 0; gi < NL; gi++) {
                 const double c = ring_ag[(rp * K + e_exp) * NL + gi];
-                if (c == 0.0) continue;
+                if (is_zero(c)) continue;
                 const double* gv = a.gv + (size_t)a.live[gi] * CP * L + li;
 #pragma unroll
                 for (int e = 0; e < CP; e++) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);
@@ -897,7 +897,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_shfl(const BatchArgs a) {
             for (int e = 0; e < P; e++) om[e] = __ldg(o0 + (size_t)e * L);
             for (int gi = 0; gi < NL; gi++) {
                 const double c = ring_ag[(rp * K + e_exp) * NL + gi];
-                if (c == 0.0) continue;
+                if (is_zero(c)) continue;
                 const double* gv = a.gv + (size_t)a.live[gi] * P * L + li;
 #pragma unroll
                 for (int e = 0; e < P; e++) om[e] = fma(c, __ldg(gv + (size_t)e * L), om[e]);

@@ -4,6 +4,13 @@
 
 namespace sss {
 
+// x == 0.0 (either sign) tested on the integer pipe: on this GPU a double
+// comparison issues on the FP64 pipe, which the Horner terms saturate.  The
+// same result as x == 0.0 for every x (a NaN is not zero).
+__device__ __forceinline__ bool is_zero(double x) {
+    return (__double_as_longlong(x) << 1) == 0;
+}
+
 // Node time of Gauss-Legendre node `node` in fine step r of output sample
 // t, in the reference's operation order (generate_simulator.py:158-167,
 // 1954-1959): ((t0 + (r*dt)/F) + dt*t) + (dt*node)/F.  Every operation is
@@ -22,7 +29,7 @@ __device__ __forceinline__ double node_time(double t0, double dt, int F, int r,
 // argument is rounded step by step as Python's math.tau*f*t + phase is.
 __device__ __forceinline__ double segment_value(const double* s, double t) {
     double a = s[2];
-    if (a == 0.0) return s[1];
+    if (is_zero(a)) return s[1];
     double arg = __dadd_rn(__dmul_rn(__dmul_rn(6.283185307179586, s[3]), t), s[4]);
     return __dadd_rn(s[1], __dmul_rn(a, cos(arg)));
 }

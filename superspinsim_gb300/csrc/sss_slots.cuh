@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(256, 1) k_batch_slots(const BatchArgs a) {
             for (int q = 0; q < S; q++) om[q] = __ldg(o0 + (size_t)q * L);
             for (int gi = 0; gi < NL; gi++) {
                 const double c = ring_ag[(rp * K + e_exp) * NL + gi];
-                if (c == 0.0) continue;
+                if (is_zero(c)) continue;
                 const double* gv = a.gv + (size_t)a.live[gi] * S * L + li;
                 const unsigned am = a.amask[gi];
 #pragma unroll
