@@ -309,7 +309,8 @@ int sss_plan_last_launches(const sss_plan* plan);
  * that start from parked partial sums, every chain starting at a fixed
  * slot, 8, 16 or 32 lanes).  Automatic lanes: per lane count the cheapest
  * layout (FP64 instructions per Horner term), and the lane count whose
- * busiest SM sub-partition issues the fewest of them.  No
+ * busiest SM sub-partition issues the fewest of them.  Configured lanes
+ * also set the row-part adjoint's forward and backward groups.  No
  * reference counterpart (the reference's launch shapes are fixed,
  * generate_simulator.py:85-106). */
 int sss_plan_set_batch_config(sss_plan* plan, int lanes, int cta_threads,

@@ -793,6 +793,7 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
         long parts4 = 0;
         for (const auto& re : rowsT) parts4 += std::max<long>(1, ((long)re.size() + 3) / 4);
         for (int Lc : {16, 32, 64, 128, 256}) {
+            if (p->batch_lanes > 0 && Lc != p->batch_lanes) continue;  // configured lanes
             if (Lb && Lc > 2 * parts4) break;
             BatchLayout trial;
             if (parts_layout_rows(p, rowsT, prioT, Lc, Lc > 32 ? Lc : 32, 3, 2, Ly.active,

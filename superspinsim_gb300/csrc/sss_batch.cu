@@ -2149,7 +2149,7 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
         };
         // lanes as configured, or the automatic count (auto_lanes)
         int rc = SSS_EINVAL, chosen = 0;
-        if (p->batch_lanes > 0 && !force_parts) {
+        if (p->batch_lanes > 0) {
             chosen = L;
         } else {
             const long n_rule = p->auto_lanes_ntraj > 0 ? p->auto_lanes_ntraj : ntraj;

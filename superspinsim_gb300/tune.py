@@ -31,7 +31,11 @@ def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, re
              lanes=(0, 8, 16, 32, 64, 128), variants=(1, 3, 4, 6, 7), threads=(32, 64, 128),
              chunks=(1, 4, 16, 64), chunk_tolerance=0.01, use_cache=True):
     """Pick and set the fastest batch configuration for this sweep and batch,
-    then its launch length.  Returns {"config": (lanes, variant, threads),
+    then its launch length.  With uneven sample counts the lanes stay
+    automatic (candidates other than 0 are dropped): a batch of uneven
+    lengths runs in phases that widen the lane groups as trajectories
+    finish, which only automatic lanes do, and probes of the first samples
+    cannot see that gain.  Returns {"config": (lanes, variant, threads),
     "ms_per_traj_step": ..., "trials": [...], "samples_per_launch": c,
     "chunk_trials": [...]}: c is the shortest candidate launch length (in
     output samples) whose time over a window of max(chunks) samples is
@@ -44,7 +48,10 @@ def autotune(sweep, rho0, programs, time_step, samples=None, probe_samples=2, re
     if flat.shape[0] == 1 and progs.shape[0] > 1:
         flat = np.repeat(flat, progs.shape[0], axis=0)
     B = flat.shape[0]
-    key = _key(sweep, B, progs)
+    uneven = samples is not None and np.unique(np.asarray(samples)).size > 1
+    if uneven:
+        lanes = (0,)
+    key = _key(sweep, B, progs) + (uneven,)
     if use_cache and key in _CACHE:
         best = _CACHE[key]
         L, var, th = best["config"]
