@@ -414,8 +414,11 @@ int launch_adj(sss_plan* p, const AdjArgs& a, int threads, size_t smem, int grid
 // part so that only the first `ngx` positions carry the third FMA.  The x
 // channel's coefficients and derivative factors (cos, -a sin and segment at
 // every node) come from a ring filled kRing steps at a time, walking back.
-// Gradient sums are kept per node and segment in registers of lane 0 and
-// added to the output when the segment changes.
+// Gradient sums are kept per node and segment in registers of every lane
+// (its share of g) and summed over the group and added to the output only
+// when the node's segment changes.  The stored state before an exponential
+// is loaded when the exponential starts, so its latency hides behind the
+// series.
 struct AdjPartsArgs {
     int M, K, Q, F, nch, nseg, ntraj, degree, T;
     long n_steps;
@@ -476,6 +479,12 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
     for (int k = 0; k < kCloseMax; k++) cw[k] = __ldg(a.cw + (size_t)k * L + li);
     const int kc = a.kc, ngx = a.ngx;
     const int r0 = __ldg(a.rbeg + li), r1 = __ldg(a.rbeg + li + 1);
+    // positions of this lane's first rows in the stored forward states: their
+    // values are loaded when an exponential starts and used after its series
+    constexpr int kPre = 4;
+    int fpos[kPre];
+#pragma unroll
+    for (int i = 0; i < kPre; i++) fpos[i] = r0 + i < r1 ? __ldg(a.fwdpos + r0 + i) : 0;
     __syncthreads();
 
     // a group of L <= 32 lanes lives in one warp; a wider one is the CTA
@@ -532,7 +541,9 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
         }
         const double* dprog = prog + (size_t)a.dch * a.nseg * 5;
         double* gb = a.grad + (size_t)b * a.nseg * a.npar;
-        // lane 0: running gradient sums per node, for segment cur_seg[k]
+        // every lane: its share of the running gradient sums per node, for
+        // segment cur_seg[k] (the same in every lane); summed over the group
+        // only when the node's segment changes
         int cur_seg[kMaxQ];
         double acc_a[kMaxQ], acc_p[kMaxQ], acc_o[kMaxQ], acc_f[kMaxQ];
 #pragma unroll
@@ -543,6 +554,26 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
             acc_o[k] = 0.0;
             acc_f[k] = 0.0;
         }
+        // node k's sums over the group into its segment's gradient entries,
+        // then zero (every lane calls it together)
+        auto flush = [&](int k) {
+            const double ta = gsum(acc_a[k]), tp = gsum(acc_p[k]);
+            double to = 0.0, tf = 0.0;
+            if (a.npar == 4) {
+                to = gsum(acc_o[k]);
+                tf = gsum(acc_f[k]);
+            }
+            if (li == 0) {
+                double* gs = gb + (size_t)a.npar * cur_seg[k];
+                gs[0] += ta;
+                gs[1] += tp;
+                if (a.npar == 4) {
+                    gs[2] += to;
+                    gs[3] += tf;
+                }
+            }
+            acc_a[k] = acc_p[k] = acc_o[k] = acc_f[k] = 0.0;
+        };
         for (int row = r0; row < r1; row++) mu[row] = 0.0;
         gsync();
         const double* st_b = a.states + (size_t)b * a.n_steps * K * M;
@@ -604,6 +635,10 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                 rp = 0;
             }
             for (int e_exp = 0; e_exp < K; e_exp++) {
+                const double* rb = st_b + ((size_t)n * K + e_exp) * M;
+                double rbv[kPre];
+#pragma unroll
+                for (int i = 0; i < kPre; i++) rbv[i] = r0 + i < r1 ? __ldg(rb + fpos[i]) : 0.0;
                 const double* o0 = a.om0 + (size_t)e_exp * CP * L + li;
 #pragma unroll
                 for (int e = 0; e < CP; e++) om[e] = __ldg(o0 + (size_t)e * L);
@@ -620,11 +655,14 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                 double* pyn = yA;
                 for (int j = d; j >= 1; j--) {
                     const double ij = a.inv_j[j];
-                    double s1[C], s2[C];
+                    // three independent chains per part: Omega^T px, G^T py
+                    // (the first ngx entries) and Omega^T py
+                    double s1[C], s2[C], s3[C];
 #pragma unroll
                     for (int c = 0; c < C; c++) {
                         s1[c] = 0.0;
                         s2[c] = 0.0;
+                        s3[c] = 0.0;
                     }
 #pragma unroll
                     for (int q = 0; q < P; q++)
@@ -634,11 +672,11 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                             const double yv = pyc[col[e]];
                             s2[c] = fma(om[e], yv, s2[c]);
                             s1[c] = fma(om[e], pxc[col[e]], s1[c]);
-                            if (q < ngx) s1[c] = fma(gx[e], yv, s1[c]);
+                            if (q < ngx) s3[c] = fma(gx[e], yv, s3[c]);
                         }
 #pragma unroll
                     for (int c = 0; c < C; c++) {
-                        parts1[li * C + c] = s1[c];
+                        parts1[li * C + c] = s1[c] + s3[c];
                         parts2[li * C + c] = s2[c];
                     }
                     gsync();
@@ -660,62 +698,40 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                     pxn = (pxn == xA) ? xB : xA;
                     pyn = (pyn == yA) ? yB : yA;
                 }
-                // g = rho_before . px;  mu <- E^T mu (the buffer holding it)
-                const double* rb = st_b + ((size_t)n * K + e_exp) * M;
+                // this lane's share of g = rho_before . px;  mu <- E^T mu (the
+                // buffer holding it)
                 double g = 0.0;
-                for (int row = r0; row < r1; row++) g = fma(rb[__ldg(a.fwdpos + row)], pxc[row], g);
-                g = gsum(g);
+#pragma unroll
+                for (int i = 0; i < kPre; i++)
+                    if (r0 + i < r1) g = fma(rbv[i], pxc[r0 + i], g);
+                for (int row = r0 + kPre; row < r1; row++) g = fma(rb[__ldg(a.fwdpos + row)], pxc[row], g);
                 double* newmu = const_cast<double*>(pyc);
                 if (newmu == yA) yA = mu; else yB = mu;
                 mu = newmu;
-                if (li == 0) {
 #pragma unroll
-                    for (int k = 0; k < kMaxQ; k++) {
-                        if (k >= Q) break;
-                        const double* rd = ring_d + (rp * Q + k) * 4;
-                        const int sg = (int)rd[2];
-                        if (sg != cur_seg[k]) {
-                            if (cur_seg[k] >= 0) {
-                                double* gs = gb + (size_t)a.npar * cur_seg[k];
-                                gs[0] += acc_a[k];
-                                gs[1] += acc_p[k];
-                                if (a.npar == 4) {
-                                    gs[2] += acc_o[k];
-                                    gs[3] += acc_f[k];
-                                }
-                            }
-                            cur_seg[k] = sg;
-                            acc_a[k] = 0.0;
-                            acc_p[k] = 0.0;
-                            acc_o[k] = 0.0;
-                            acc_f[k] = 0.0;
-                        }
-                        if (sg >= 0) {
-                            const double hw = a.h * __ldg(a.W + e_exp * Q + k);
-                            acc_a[k] = fma(hw * rd[0], g, acc_a[k]);
-                            acc_p[k] = fma(hw * rd[1], g, acc_p[k]);
-                            acc_o[k] = fma(hw, g, acc_o[k]);
-                            acc_f[k] = fma(hw * rd[3], g, acc_f[k]);
-                        }
+                for (int k = 0; k < kMaxQ; k++) {
+                    if (k >= Q) break;
+                    const double* rd = ring_d + (rp * Q + k) * 4;
+                    const int sg = (int)rd[2];
+                    if (sg != cur_seg[k]) {  // the same in every lane of the group
+                        if (cur_seg[k] >= 0) flush(k);
+                        cur_seg[k] = sg;
+                    }
+                    if (sg >= 0) {
+                        const double hw = a.h * __ldg(a.W + e_exp * Q + k);
+                        acc_a[k] = fma(hw * rd[0], g, acc_a[k]);
+                        acc_p[k] = fma(hw * rd[1], g, acc_p[k]);
+                        acc_o[k] = fma(hw, g, acc_o[k]);
+                        acc_f[k] = fma(hw * rd[3], g, acc_f[k]);
                     }
                 }
                 gsync();
             }
             rp++;
         }
-        if (li == 0) {
 #pragma unroll
-            for (int k = 0; k < kMaxQ; k++)
-                if (k < Q && cur_seg[k] >= 0) {
-                    double* gs = gb + (size_t)a.npar * cur_seg[k];
-                    gs[0] += acc_a[k];
-                    gs[1] += acc_p[k];
-                    if (a.npar == 4) {
-                        gs[2] += acc_o[k];
-                        gs[3] += acc_f[k];
-                    }
-                }
-        }
+        for (int k = 0; k < kMaxQ; k++)
+            if (k < Q && cur_seg[k] >= 0) flush(k);
         gsync();
     }
 }
