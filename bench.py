@@ -325,7 +325,7 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def adjoint_workload(nv21=False, n_traj=0):
+def adjoint_workload(nv21=False, n_traj=0, n_seg=0, readout=300e-9):
     """Pulse-shape objective of the adjoint workloads: NV-7 at 5 mT, 256
     seeded shapes of 128 piecewise-constant segments of 2 ns (Rabi 0-20 MHz,
     phase 0-2pi, carrier at the ms=0 -> +1 line), or NV-21 (14N) at 50 mT,
@@ -341,21 +341,21 @@ def adjoint_workload(nv21=False, n_traj=0):
                                             params=models.nv21_params())
         g, vm = generate_atoms(spins, inter, groups, use_incoherent=False)
         gens = np.array([g["generators"][k] for k in ("L0", "Gx", "Gy", "Gz", "Gr")])
-        B, S, f_c = n_traj or 32, 64, 2.870e9 + GAMMA*0.05
+        B, S, f_c = n_traj or 32, n_seg or 64, 2.870e9 + GAMMA*0.05
         rho = np.zeros((21, 21), complex)
         for k in range(3, 6):
             rho[k, k] = 1/3
         levels = list(range(9, 18))
     else:
         gens, vm = nv7_model()
-        B, S, f_c = n_traj or 256, 128, F_RES
+        B, S, f_c = n_traj or 256, n_seg or 128, F_RES
         rho = np.zeros((7, 7), complex)
         rho[1, 1] = 1.0
         levels = [3, 4, 5]
     rng = np.random.default_rng(20260104)
     rabi = rng.uniform(0, 20e6, (B, S))
     phase = rng.uniform(0, 2*np.pi, (B, S))
-    progs, dur = protocols.pulse_shapes(rabi, phase, 2e-9, f_c, LASER, 300e-9)
+    progs, dur = protocols.pulse_shapes(rabi, phase, 2e-9, f_c, LASER, readout)
     T = int(round(dur[0]/DT_OUT))
     tw = trapezoid_weights(T, DT_OUT, S*2 - 1, T - 1)
     obj = Objective(gens, vm, rho, levels, 65.9e6, number_of_exponentials=K_EXP,
@@ -417,7 +417,8 @@ def run_adjoint_workload(args, rank, world):
     """Times the checkpointed adjoint (objective + 2S gradients per shape)
     of adjoint_workload against one forward solve of the same batch."""
     import torch
-    obj, progs, T, tw, S, name = adjoint_workload(args.workload == "adjoint-nv21", args.n_traj)
+    obj, progs, T, tw, S, name = adjoint_workload(args.workload == "adjoint-nv21", args.n_traj,
+                                                  args.segments, args.readout)
     B = progs.shape[0]
     for _ in range(args.warmup):
         obj.run(progs, DT_OUT, T, tw)
@@ -436,8 +437,9 @@ def run_adjoint_workload(args, rank, world):
             "unit": f"gradients/s ({2*S} parameters each)", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3*adj_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{B} pulse shapes x {S} segments of 2 ns + 300 ns readout, "
-                                   f"{name}, dt 5 ps ({T*F:,} steps each)",
+            "config": {"workload": f"{B} pulse shapes x {S} segments of 2 ns + "
+                                   f"{args.readout*1e9:g} ns readout, {name}, dt 5 ps "
+                                   f"({T*F:,} steps each)",
                        "parameters_per_shape": 2*S, "traj_steps": steps},
             "adjoint_over_forward": adj_s/fwd_s,
             "forward_traj_steps_per_s": steps/fwd_s,
@@ -462,6 +464,10 @@ def main():
     ap.add_argument("--workload", default="odmr",
                     choices=["odmr", "ramsey", "nv21", "adjoint", "adjoint-nv21"])
     ap.add_argument("--n-traj", type=int, default=0)
+    ap.add_argument("--segments", type=int, default=0,
+                    help="adjoint workloads: pulse segments per shape (default 128, NV-21 64)")
+    ap.add_argument("--readout", type=float, default=300e-9,
+                    help="adjoint workloads: laser readout after the pulses (s)")
     ap.add_argument("--graph-chunk", type=int, default=0,
                     help="time a CUDA graph of the prepared run in chunks of this many output "
                          "samples (resumable launches) instead of one launch")
