@@ -56,7 +56,7 @@ constexpr int kAdjMaxTaylor = 24;
 
 struct AdjArgs {
     int M, Ga, K, Q, F, nch, nseg, ntraj, degree, N, E, ET;
-    int xg;          // position of Gx among the active generators
+    int xg;          // position of Gx (the differentiated channel's generator) among the active ones
     int dch, npar;   // differentiated channel; parameters per segment (2 or 4)
     long n_steps;    // fine steps per trajectory
     int T, C, n_ck;
@@ -88,7 +88,7 @@ struct AdjArgs {
 
 __device__ __forceinline__ int wcol(unsigned w) { return (int)(w & 0xffffu); }
 __device__ __forceinline__ int wend(unsigned w) { return (int)(w >> 16); }
-// transposed-entry index flag: the x generator is non-zero at this entry
+// transposed-entry index flag: the differentiated generator is non-zero here
 constexpr int kHasG = 1 << 30;
 
 // segment of a channel's program (prog points at the channel) at time t,
@@ -411,9 +411,10 @@ int launch_adj(sss_plan* p, const AdjArgs& a, int threads, size_t smem, int grid
 // from px = 0, py = mu: then py = E^T mu (the new adjoint) and
 // g = rho_before . px = mu^T L(Omega, G) rho_before.  Per entry three FMAs
 // (two chains share the gathered py value); G^T entries sit first in each
-// part so that only the first `ngx` positions carry the third FMA.  The x
-// channel's coefficients and derivative factors (cos, -a sin and segment at
-// every node) come from a ring filled kRing steps at a time, walking back.
+// part so that only the first `ngx` positions carry the third FMA.  The
+// differentiated channel's coefficients and derivative factors (cos, -a sin,
+// segment and -a sin tau t at every node) come from a ring filled kRing
+// steps at a time, walking back.
 // Gradient sums are kept per node and segment in registers of every lane
 // (its share of g) and summed over the group and added to the output only
 // when the node's segment changes.  The stored state before an exponential
@@ -431,7 +432,7 @@ struct AdjPartsArgs {
     const unsigned* cw;     // kCloseMax*L close words [k][l]
     const double* om0;      // K*C*P*L constant part of Omega^T per exponential
     const double* gv;       // Ga*C*P*L transposed generator values [g][e][l]
-    const double* gx;       // C*P*L  x generator values (the G of the series)
+    const double* gx;       // C*P*L  differentiated generator's values (the G of the series)
     const int* rbeg;        // L+1
     const int* fwdpos;      // M: index of each row in the stored forward states
     const double* rw;       // M
