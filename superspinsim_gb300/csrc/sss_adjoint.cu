@@ -46,6 +46,7 @@
 #include <cmath>
 #include <vector>
 
+#include "sss_adjoint_slots.cuh"
 #include "sss_device.cuh"
 #include "sss_internal.cuh"
 
@@ -763,6 +764,175 @@ int launch_adj_parts(sss_plan* p, int C, int P, const AdjPartsArgs& a, int threa
 // over trajectory chunks sized to the free device memory.  Returns
 // SSS_EINVAL (with nothing launched) when the pattern does not fit the
 // row-part kernels or the states of one trajectory do not fit in memory.
+// The slot-programmed backward (sss_adjoint_slots.cu): the block matrix
+// [[Omega^T, G^T], [0, Omega^T]] of the forward layout's rows, 2M block rows
+// -- px of row c holds the Omega^T entries (Omega[r][c], column r) and the
+// G^T entries (G[r][c], column M + r), py of row c the Omega^T entries
+// (column M + r) -- laid out by the forward kernels' phased or slot-packed
+// packer at 32 lanes, with bank-aware placement.  Builds the kernel's
+// tables into p->w_adjb and its arguments (the per-chunk pointers are set at
+// launch); SSS_EINVAL, with nothing uploaded, when the block fits neither
+// program.
+static int adjoint_slots_prepare(sss_plan* p, const BatchLayout& Ly, int gd, int xg, double t0,
+                                 double dt, int T, int F, int nch, int nseg, const double* h_rw,
+                                 const double* h_tw, int dch, int npar, AdjSlotArgs* out,
+                                 BatchLayout* BLo, size_t* smem_out, int* threads_out,
+                                 cudaStream_t st) {
+    const SparseGenerators& sp = p->sparse;
+    const int M = Ly.M, Ga = Ly.Ga, K = p->d.K, Q = p->d.Q;
+    const int L = 32, threads = 32;
+    if (2 * M + 2 > (int)kSlotIdx) return fail(SSS_EINVAL, "block series too large for slot words");
+    std::vector<std::vector<BatchLayout::Ent>> brows(2 * (size_t)M);
+    p->slot_consts.clear();
+    for (int r = 0; r < M; r++)
+        for (const BatchLayout::Ent& en : Ly.row_ents[r]) {
+            brows[en.col].push_back({r, en.q});
+            brows[(size_t)M + en.col].push_back({M + r, en.q});
+            const double gval = sp.val[(size_t)gd * sp.nnz + en.q];
+            if (gval != 0.0) {
+                brows[en.col].push_back({M + r, sp.nnz + (int)p->slot_consts.size()});
+                p->slot_consts.push_back(gval);
+            }
+        }
+    // generators assembled every exponential: the differentiated one and
+    // those whose channel varies
+    std::vector<char> varies(sp.G, 0);
+    std::vector<int> live;
+    int x_live = -1;
+    for (int gi = 0; gi < Ga; gi++) {
+        const int g = Ly.active[gi];
+        if (g != 0 && (g == gd || !Ly.chan_const[g])) {
+            varies[g] = 1;
+            if (gi == xg) x_live = (int)live.size();
+            live.push_back(gi);
+        }
+    }
+    std::vector<int> brr(2 * (size_t)M);
+    for (int i = 0; i < 2 * M; i++) brr[i] = i;
+    BatchLayout& BL = *BLo;
+    int rc = phased_layout_rows(p, brows, L, threads, kSlotsMax, Ly.active, brr, varies, &BL);
+    if (rc != SSS_OK) {
+        set_error("");
+        rc = slots_layout_rows(p, brows, L, threads, kSlotsMax, Ly.active, brr, &BL);
+    }
+    if (rc != SSS_OK) return rc;
+    BL.M = 2 * M;
+    BL.Ga = Ga;
+    BL.active = Ly.active;
+    if (int rc2 = place_banks(p, BL, Ly.active, varies)) return rc2;
+    const int S = BL.S, Ms = 2 * M + 2 + BL.npart, NL = (int)live.size();
+    if (NL > kMaxG) return fail(SSS_EINVAL, "too many live generators");
+    // the constant part of the block per exponential: the folded generators,
+    // 1 for partial adds, the G^T values for constant entries
+    const double h = dt / F;
+    const size_t SL = (size_t)S * L;
+    std::vector<double> om0((size_t)K * SL, 0.0);
+    for (int gi = 0; gi < Ga; gi++) {
+        if (std::find(live.begin(), live.end(), gi) != live.end()) continue;
+        const int g = Ly.active[gi];
+        const double X = g == 0 ? 1.0 : Ly.chan_value[g];
+        for (int e = 0; e < K; e++) {
+            double s = 0.0;
+            for (int k = 0; k < Q; k++) s = std::fma(p->W[e * Q + k], X, s);
+            const double ag = s * h;
+            for (size_t i = 0; i < SL; i++) {
+                double& o = om0[(size_t)e * SL + i];
+                o = std::fma(ag, BL.gv[(size_t)gi * SL + i], o);
+            }
+        }
+    }
+    for (int e = 0; e < K; e++)
+        for (size_t i = 0; i < SL; i++) {
+            if (BL.entry_q[i] == -2) om0[(size_t)e * SL + i] = 1.0;
+            if (BL.entry_q[i] == -3) om0[(size_t)e * SL + i] = BL.cval[i];
+        }
+    std::vector<int> ppx(M), ppy(M), fpos(M);
+    std::vector<double> rw(M, 0.0), tw(h_tw, h_tw + T), toff(F), noff(Q);
+    for (int i = 0; i < M; i++) {
+        ppx[i] = BL.newpos[i];
+        ppy[i] = BL.newpos[(size_t)M + i];
+        fpos[i] = Ly.newpos[i];
+        if (h_rw) rw[i] = h_rw[Ly.row_orig[Ly.newpos[i]]];
+    }
+    for (int r = 0; r < F; r++) toff[r] = ((double)r * dt) / F;
+    for (int k = 0; k < Q; k++) noff[k] = (dt * p->nodes[k]) / F;
+    // blob: gv | om0 | rw | tw | toff | noff | cw | ppx | ppy | fpos
+    std::vector<double> dbl(BL.gv);
+    const size_t o_om0 = dbl.size();
+    dbl.insert(dbl.end(), om0.begin(), om0.end());
+    const size_t o_rw = dbl.size();
+    dbl.insert(dbl.end(), rw.begin(), rw.end());
+    const size_t o_tw = dbl.size();
+    dbl.insert(dbl.end(), tw.begin(), tw.end());
+    const size_t o_toff = dbl.size();
+    dbl.insert(dbl.end(), toff.begin(), toff.end());
+    const size_t o_noff = dbl.size();
+    dbl.insert(dbl.end(), noff.begin(), noff.end());
+    std::vector<int> ints(BL.cw.begin(), BL.cw.end());
+    const size_t o_px = ints.size();
+    ints.insert(ints.end(), ppx.begin(), ppx.end());
+    const size_t o_py = ints.size();
+    ints.insert(ints.end(), ppy.begin(), ppy.end());
+    const size_t o_fp = ints.size();
+    ints.insert(ints.end(), fpos.begin(), fpos.end());
+    const size_t bytes = sizeof(double) * dbl.size() + sizeof(int) * ints.size();
+    if (int rc2 = p->w_adjb.ensure(bytes + 64)) return rc2;
+    {
+        std::vector<char> blob(bytes);
+        memcpy(blob.data(), dbl.data(), sizeof(double) * dbl.size());
+        memcpy(blob.data() + sizeof(double) * dbl.size(), ints.data(), sizeof(int) * ints.size());
+        SSS_CUDA(cudaMemcpyAsync(p->w_adjb.p, blob.data(), bytes, cudaMemcpyHostToDevice, st));
+        SSS_CUDA(cudaStreamSynchronize(st));  // the host blob goes out of scope
+    }
+    const double* dv = p->w_adjb.as<double>();
+    const int* di = reinterpret_cast<const int*>(dv + dbl.size());
+    AdjSlotArgs a{};
+    a.M = M;
+    a.M2 = 2 * M;
+    a.Ms = Ms;
+    a.K = K; a.Q = Q; a.F = F; a.nch = nch; a.nseg = nseg; a.degree = Ly.degree; a.T = T;
+    a.n_steps = (long)T * F;
+    a.h = h; a.t0 = t0; a.dt = dt;
+    a.n_live = NL;
+    a.x_live = x_live;
+    a.dch = dch;
+    a.npar = npar;
+    for (int i = 0; i < NL; i++) a.live[i] = live[i];
+    for (int gi = 0; gi < Ga; gi++) a.gen_index[gi] = Ly.active[gi];
+    for (int i = 0; i < NL; i++) {
+        unsigned m = 0;
+        for (int q = 0; q < S; q++)
+            for (int l = 0; l < L; l++)
+                if (BL.gv[((size_t)live[i] * S + q) * L + l] != 0.0) m |= 1u << q;
+        a.amask[i] = m;
+    }
+    a.cw = reinterpret_cast<const unsigned*>(di);
+    a.gv = dv;
+    a.om0 = dv + o_om0;
+    a.rw = dv + o_rw;
+    a.tw = dv + o_tw;
+    a.toff = dv + o_toff;
+    a.noff = dv + o_noff;
+    a.ppx = di + o_px;
+    a.ppy = di + o_py;
+    a.fpos = di + o_fp;
+    a.W = p->d_gens.as<double>() + p->gens.size();
+    for (int j = 0; j <= kMaxTaylor; j++) a.cfac[j] = 0.0;
+    for (int j = 1; j <= Ly.degree; j++) {
+        double c = 1.0;
+        for (int k = j; k <= Ly.degree; k++) c *= k;
+        a.cfac[j] = c;
+    }
+    a.inv_dfact = 1.0 / a.cfac[1];
+    const size_t per_slot = ((3 * (size_t)Ms + (size_t)kRing * (Q * NL + K * NL + 4 * Q)) | 1);
+    const size_t smem = sizeof(double) * (per_slot * (threads / L) + M);
+    if (smem > 227 * 1024) return fail(SSS_EINVAL, "slot adjoint kernel: shared memory per CTA too large");
+    *out = a;
+    *smem_out = smem;
+    *threads_out = threads;
+    return SSS_OK;
+}
+
 int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                       const double* d_prog, double t0, double dt, int T, int F,
                       const double* h_rw, const double* h_tw, int dch, int npar, double* d_J,
@@ -789,6 +959,68 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
     const size_t budget = p->adj_max_bytes ? p->adj_max_bytes : free_b / 2;
     if (per_traj > budget) return fail(SSS_EINVAL, "adjoint states of one trajectory exceed memory");
     const int chunk = (int)std::min<size_t>((size_t)ntraj, budget / per_traj);
+
+    // ---- the slot-programmed backward, where the block series fits ----
+    if (p->batch_variant != 4 && p->batch_variant != 5 && Ly.degree <= kMaxTaylor) {
+        AdjSlotArgs sa{};
+        BatchLayout BL;
+        size_t smem = 0;
+        int threads = 0;
+        const int rc = adjoint_slots_prepare(p, Ly, gd, xg, t0, dt, T, F, nch, nseg, h_rw, h_tw,
+                                             dch, npar, &sa, &BL, &smem, &threads, st);
+        if (rc == SSS_OK) {
+            PartsForward fw;
+            if (int rc2 = parts_forward_prepare(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {gd},
+                                                p->w_adjf, &fw, st))
+                return rc2;
+            if (int rc2 = p->w_states.ensure(per_traj * chunk)) return rc2;
+            if (int rc2 = p->w_adjro.ensure(sizeof(double) * (size_t)chunk * T)) return rc2;
+            if (int rc2 = p->w_adjst.ensure(sizeof(double) * (size_t)chunk * N)) return rc2;
+            if (int rc2 = p->w_queue.ensure(sizeof(int) * 4)) return rc2;
+            SSS_CUDA(cudaMemsetAsync(d_J, 0, sizeof(double) * ntraj, st));
+            SSS_CUDA(cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ntraj * nseg * npar, st));
+            if (!p->ev_begin) {
+                SSS_CUDA(cudaEventCreate(&p->ev_begin));
+                SSS_CUDA(cudaEventCreate(&p->ev_end));
+            }
+            SSS_CUDA(cudaEventRecord(p->ev_begin, st));
+            int launches = 0;
+            for (int b0 = 0; b0 < ntraj; b0 += chunk) {
+                const int nb = std::min(chunk, ntraj - b0);
+                double* state = p->w_adjst.as<double>();
+                const double* prog = d_prog + (size_t)b0 * nch * nseg * 5;
+                SSS_CUDA(cudaMemcpyAsync(state, d_rho0 + (size_t)b0 * N, sizeof(double) * (size_t)nb * N,
+                                         cudaMemcpyDeviceToDevice, st));
+                if (int rc2 = parts_forward_launch(p, fw, nb, state, prog, t0, T, p->w_adjro.as<double>(),
+                                                   p->w_states.as<double>(), st))
+                    return rc2;
+                AdjSlotArgs ab = sa;
+                ab.ntraj = nb;
+                ab.states = p->w_states.as<double>();
+                ab.readout = p->w_adjro.as<double>();
+                ab.prog = prog;
+                ab.J = d_J + b0;
+                ab.grad = d_grad + (size_t)b0 * nseg * npar;
+                ab.queue = p->w_queue.as<int>();
+                SSS_CUDA(cudaMemsetAsync(ab.queue, 0, sizeof(int), st));
+                if (int rc2 = launch_adjoint_slots(p, BL.L, BL.phased, BL.shape, BL.S, ab, threads, smem, st))
+                    return rc2;
+                launches += 2;
+            }
+            SSS_CUDA(cudaEventRecord(p->ev_end, st));
+            p->ev_recorded = true;
+            p->last_launches = launches;
+            p->last_batch_lanes = BL.L;
+            p->last_degree = Ly.degree;
+            p->last_substeps = 1;
+            p->last_rows = M;
+            p->last_nnz = (int)Ly.nnz;
+            p->last_variant = BL.phased ? 7 : 6;
+            return SSS_OK;
+        }
+        if (rc != SSS_EINVAL) return rc;
+        set_error("");
+    }
 
     // ---- backward layout: the transposed pattern, x-generator entries first ----
     std::vector<int> rows_reached(M);

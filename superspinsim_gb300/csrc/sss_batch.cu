@@ -1474,6 +1474,7 @@ static int emit_slot_cells(sss_plan* p, const std::vector<std::vector<BatchLayou
     const unsigned zero_row = (unsigned)M, sink = (unsigned)M + 1;
     Ly.cw.assign((size_t)2 * S * L, 0u);
     Ly.entry_q.assign((size_t)S * L, -1);
+    Ly.cval.assign((size_t)S * L, 0.0);
     Ly.gv.assign((size_t)Ga * S * L, 0.0);
     for (int l = 0; l < L; l++)
         for (int q = 0; q < S; q++) {
@@ -1483,9 +1484,14 @@ static int emit_slot_cells(sss_plan* p, const std::vector<std::vector<BatchLayou
             if (c.kind == 1) {
                 const BatchLayout::Ent& en = rows[c.row][c.ent];
                 ld = (unsigned)newpos[en.col];
-                Ly.entry_q[idx] = en.q;
-                for (int gi = 0; gi < Ga; gi++)
-                    Ly.gv[((size_t)gi * S + q) * L + l] = sp.val[(size_t)active[gi] * sp.nnz + en.q];
+                if (en.q >= sp.nnz) {  // a constant entry
+                    Ly.entry_q[idx] = -3;
+                    Ly.cval[idx] = p->slot_consts[(size_t)(en.q - sp.nnz)];
+                } else {
+                    Ly.entry_q[idx] = en.q;
+                    for (int gi = 0; gi < Ga; gi++)
+                        Ly.gv[((size_t)gi * S + q) * L + l] = sp.val[(size_t)active[gi] * sp.nnz + en.q];
+                }
             } else if (c.kind == 2) {
                 ld = kLdNext | (unsigned)(M + 2 + c.part);
                 Ly.entry_q[idx] = -2;
@@ -1655,13 +1661,14 @@ static int bank_relabel(sss_plan* p, BatchLayout& Ly, const std::vector<int>& ac
     {
         const std::vector<unsigned> cw0(cw);
         const std::vector<int> eq0(Ly.entry_q);
-        const std::vector<double> gv0(Ly.gv);
+        const std::vector<double> gv0(Ly.gv), cv0(Ly.cval);
         for (int c = 0; c < n_load; c++) {
             const int o = origin[c];
             if (o == c) continue;
             const int q = c / L, l = c % L, qo = o / L;
             cw[(size_t)q * L + l] = cw0[(size_t)qo * L + l];
             Ly.entry_q[(size_t)q * L + l] = eq0[(size_t)qo * L + l];
+            if (!cv0.empty()) Ly.cval[(size_t)q * L + l] = cv0[(size_t)qo * L + l];
             for (int gi = 0; gi < Ga; gi++)
                 Ly.gv[((size_t)gi * S + q) * L + l] = gv0[((size_t)gi * S + qo) * L + l];
         }
@@ -1688,6 +1695,11 @@ static int bank_relabel(sss_plan* p, BatchLayout& Ly, const std::vector<int>& ac
             Ly.lane_of[l].push_back(inv[k]);
     Ly.npart = (M + 2 + np + 15) / 16 * 16 - (M + 2);
     return SSS_OK;
+}
+
+int place_banks(sss_plan* p, BatchLayout& Ly, const std::vector<int>& active,
+                const std::vector<char>& varies) {
+    return bank_relabel(p, Ly, active, varies);
 }
 
 static void set_slot_fields(BatchLayout& Ly, int L, int S, int SA, int npart, int threads) {
@@ -1758,7 +1770,8 @@ int phased_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::E
         for (int e = 0; e < nent[i]; e++) {
             bool var = false;
             for (int g : active)
-                var |= g < (int)varies.size() && varies[g] && sp.val[(size_t)g * sp.nnz + rows[i][e].q] != 0.0;
+                var |= rows[i][e].q < sp.nnz && g < (int)varies.size() && varies[g] &&
+                       sp.val[(size_t)g * sp.nnz + rows[i][e].q] != 0.0;
             (var ? items[i] : later).push_back(e);
         }
         items[i].insert(items[i].end(), later.begin(), later.end());

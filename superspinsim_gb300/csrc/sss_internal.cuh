@@ -69,7 +69,9 @@ struct BatchLayout {
     std::vector<int> newpos, row_orig;       // reachable -> lane order; lane order -> original
     std::vector<double> gv;                  // Ga*E*L generator values [g][e][l]
     std::vector<unsigned> words;             // E*L entry words [e][l]
-    std::vector<int> entry_q;                // E*L index into SparseGenerators (-1: padding)
+    std::vector<int> entry_q;                // E*L index into SparseGenerators (-1: padding,
+                                             // -2: partial add, -3: constant entry, value in cval)
+    std::vector<double> cval;                // E*L constant entries' values (slot layouts)
     std::vector<int> cnt;                    // entries of each lane
     // row-part variant: C parts of P entries per lane, kc close slots
     bool parts = false;
@@ -123,6 +125,10 @@ struct sss_plan {
     // after, for the last layout built, and the numberings found so far
     // (keyed by a hash of the layout's kernel words)
     int last_bank_before = 0, last_bank_after = 0;
+    // values of the constant entries of a slot layout being built: an entry
+    // whose q is sparse.nnz + k has the fixed value slot_consts[k] and no
+    // generator values (the G^T block of the adjoint's block series)
+    std::vector<double> slot_consts;
     std::unordered_map<uint64_t, std::vector<int>> bank_cache;
     int batch_variant = 0;  // 0: register variant when it fits, 2: shared-memory variant,
                             // 3: one-chain register variant, 4: row-part variant
@@ -211,6 +217,19 @@ int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg
                  const double* d_tab = nullptr, int T_tab = 0);
 int slot_layout_host(int M, const int* row_ptr, const int* col, int L, int S_cap, int* S_out,
                      int* bar_out, int* npart_out, unsigned* words, int* entries);
+// Slot-packed and phased row-part layouts of given rows (entries with q >=
+// sparse.nnz are constant entries, see sss_plan::slot_consts), and the
+// bank-aware placement of such a layout (varies[g]: generator slot g is
+// assembled every exponential).
+int slots_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows, int L,
+                      int threads, int S_cap, const std::vector<int>& active,
+                      const std::vector<int>& rows_reached, BatchLayout* out);
+int phased_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows, int L,
+                       int threads, int S_cap, const std::vector<int>& active,
+                       const std::vector<int>& rows_reached, const std::vector<char>& varies,
+                       BatchLayout* out);
+int place_banks(sss_plan* p, BatchLayout& Ly, const std::vector<int>& active,
+                const std::vector<char>& varies);
 int parts_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::Ent>>& rows,
                       const std::vector<std::vector<char>>& prio, int L, int threads, int w_chain,
                       int w_close, const std::vector<int>& active,

@@ -29,10 +29,12 @@ def _objective(name="nv7_n19"):
                      number_of_fine_divisions=100), c, rho
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 4, 1])
 def test_adjoint_objective_matches_forward_and_fd(variant):
-    """variant 0: row-part adjoint (stored forward states, transposed
-    row-part backward kernel); variant 1: the checkpointed adjoint kernel."""
+    """variant 0: stored forward states and the slot-programmed backward
+    (the block series on a phased or slot-packed program); variant 4: the
+    same forward with the transposed row-part backward kernel; variant 1:
+    the checkpointed adjoint kernel."""
     from superspinsim_gb300.adjoint import trapezoid_weights
     obj, c, rho = _objective()
     obj.plan.set_batch_config(variant=variant)
@@ -92,7 +94,7 @@ def _two_channel_problem():
     return progs, dur
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 4, 1])
 @pytest.mark.parametrize("channel", [0, 1, 3])
 def test_channel_adjoint_matches_fd(channel, variant):
     """sss_adjoint_run_channel: d J / d (amplitude, phase, offset, frequency)
