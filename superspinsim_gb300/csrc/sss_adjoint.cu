@@ -773,14 +773,16 @@ int launch_adj_parts(sss_plan* p, int C, int P, const AdjPartsArgs& a, int threa
 // tables into p->w_adjb and its arguments (the per-chunk pointers are set at
 // launch); SSS_EINVAL, with nothing uploaded, when the block fits neither
 // program.
-static int adjoint_slots_prepare(sss_plan* p, const BatchLayout& Ly, int gd, int xg, double t0,
-                                 double dt, int T, int F, int nch, int nseg, const double* h_rw,
-                                 const double* h_tw, int dch, int npar, AdjSlotArgs* out,
-                                 BatchLayout* BLo, size_t* smem_out, int* threads_out,
-                                 cudaStream_t st) {
+static int adjoint_slots_prepare(sss_plan* p, const BatchLayout& Ly, int ntraj, int gd, int xg,
+                                 double t0, double dt, int T, int F, int nch, int nseg,
+                                 const double* h_rw, const double* h_tw, int dch, int npar,
+                                 AdjSlotArgs* out, BatchLayout* BLo, size_t* smem_out,
+                                 int* threads_out, cudaStream_t st) {
     const SparseGenerators& sp = p->sparse;
     const int M = Ly.M, Ga = Ly.Ga, K = p->d.K, Q = p->d.Q;
-    const int L = 32, threads = 32;
+    // two warps per trajectory (slot-packed, 64 lanes) while the batch leaves
+    // SM sub-partitions without a warp at one warp per trajectory, else 32
+    const bool wide = (long)ntraj * 2 <= 4L * p->num_sms;
     if (2 * M + 2 > (int)kSlotIdx) return fail(SSS_EINVAL, "block series too large for slot words");
     std::vector<std::vector<BatchLayout::Ent>> brows(2 * (size_t)M);
     p->slot_consts.clear();
@@ -810,12 +812,20 @@ static int adjoint_slots_prepare(sss_plan* p, const BatchLayout& Ly, int gd, int
     std::vector<int> brr(2 * (size_t)M);
     for (int i = 0; i < 2 * M; i++) brr[i] = i;
     BatchLayout& BL = *BLo;
-    int rc = phased_layout_rows(p, brows, L, threads, kSlotsMax, Ly.active, brr, varies, &BL);
+    int rc = SSS_EINVAL;
+    if (wide) {
+        rc = slots_layout_rows(p, brows, 64, 64, 8, Ly.active, brr, &BL);
+        if (rc != SSS_OK) set_error("");
+    }
     if (rc != SSS_OK) {
-        set_error("");
-        rc = slots_layout_rows(p, brows, L, threads, kSlotsMax, Ly.active, brr, &BL);
+        rc = phased_layout_rows(p, brows, 32, 32, kSlotsMax, Ly.active, brr, varies, &BL);
+        if (rc != SSS_OK) {
+            set_error("");
+            rc = slots_layout_rows(p, brows, 32, 32, kSlotsMax, Ly.active, brr, &BL);
+        }
     }
     if (rc != SSS_OK) return rc;
+    const int L = BL.L, threads = BL.threads;
     BL.M = 2 * M;
     BL.Ga = Ga;
     BL.active = Ly.active;
@@ -966,8 +976,8 @@ int adjoint_run_parts(sss_plan* p, int ntraj, const double* d_rho0, int nch, int
         BatchLayout BL;
         size_t smem = 0;
         int threads = 0;
-        const int rc = adjoint_slots_prepare(p, Ly, gd, xg, t0, dt, T, F, nch, nseg, h_rw, h_tw,
-                                             dch, npar, &sa, &BL, &smem, &threads, st);
+        const int rc = adjoint_slots_prepare(p, Ly, ntraj, gd, xg, t0, dt, T, F, nch, nseg, h_rw,
+                                             h_tw, dch, npar, &sa, &BL, &smem, &threads, st);
         if (rc == SSS_OK) {
             PartsForward fw;
             if (int rc2 = parts_forward_prepare(p, Ly, ntraj, nch, nseg, dt, F, h_rw, {gd},

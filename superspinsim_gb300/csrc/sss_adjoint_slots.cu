@@ -294,8 +294,20 @@ int launch_adj(sss_plan* p, Kern kern, const AdjSlotArgs& a, int threads, int sl
 
 int launch_adjoint_slots(sss_plan* p, int L, bool phased, int shape, int S, const AdjSlotArgs& a,
                          int threads, size_t smem, cudaStream_t st) {
-    if (L != 32) return fail(SSS_EINVAL, "the slot adjoint runs 32-lane groups");
     const int spc = threads / L;
+    if (L == 64 && !phased) {
+        // one trajectory per 64-thread CTA: for batches too small to give
+        // every SM sub-partition a warp at 32 lanes
+        switch (S) {
+            case 5: return launch_adj(p, k_adjoint_slots<64, SlotProgram<5>>, a, threads, spc, smem, st);
+            case 6: return launch_adj(p, k_adjoint_slots<64, SlotProgram<6>>, a, threads, spc, smem, st);
+            case 7: return launch_adj(p, k_adjoint_slots<64, SlotProgram<7>>, a, threads, spc, smem, st);
+            case 8: return launch_adj(p, k_adjoint_slots<64, SlotProgram<8>>, a, threads, spc, smem, st);
+            default: return fail(SSS_EINVAL, "no 64-lane slot-packed adjoint kernel for " +
+                                                 std::to_string(S) + " slots");
+        }
+    }
+    if (L != 32) return fail(SSS_EINVAL, "the slot adjoint runs 32- or 64-lane groups");
     if (phased) {
         static_assert(kPhasedShapeCount == 8, "one case per phased shape");
 #define SSS_ADJ_PHASED(k)                                                                     \
