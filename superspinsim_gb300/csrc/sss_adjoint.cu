@@ -780,9 +780,13 @@ static int adjoint_slots_prepare(sss_plan* p, const BatchLayout& Ly, int ntraj, 
                                  int* threads_out, cudaStream_t st) {
     const SparseGenerators& sp = p->sparse;
     const int M = Ly.M, Ga = Ly.Ga, K = p->d.K, Q = p->d.Q;
-    // two warps per trajectory (slot-packed, 64 lanes) while the batch leaves
-    // SM sub-partitions without a warp at one warp per trajectory, else 32
-    const bool wide = (long)ntraj * 2 <= 4L * p->num_sms;
+    // lanes: as configured (32 or 64), else two warps per trajectory
+    // (slot-packed, 64 lanes) while the batch leaves SM sub-partitions
+    // without a warp at one warp per trajectory (measured on the C4 workload,
+    // 256 shapes: 64 lanes 1.19x faster than 32, 128 lanes no better), else 32
+    int Lw = p->batch_lanes;
+    if (Lw != 32 && Lw != 64) Lw = (long)ntraj * 2 <= 4L * p->num_sms ? 64 : 32;
+    const bool wide = Lw > 32;
     if (2 * M + 2 > (int)kSlotIdx) return fail(SSS_EINVAL, "block series too large for slot words");
     std::vector<std::vector<BatchLayout::Ent>> brows(2 * (size_t)M);
     p->slot_consts.clear();
