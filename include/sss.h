@@ -310,7 +310,11 @@ int sss_plan_last_launches(const sss_plan* plan);
  * slot, 8, 16 or 32 lanes).  Automatic lanes: per lane count the cheapest
  * layout (FP64 instructions per Horner term), and the lane count whose
  * busiest SM sub-partition issues the fewest of them.  Configured lanes
- * also set the row-part adjoint's forward and backward groups.  No
+ * also set the adjoint's forward and backward groups; for sss_adjoint_run
+ * variant 4 or 5 selects the row-part backward, the others the
+ * slot-programmed backward (the block series [[Omega^T, G^T], [0, Omega^T]]
+ * on a slot program) where it fits, and variant 1 the checkpointed
+ * adjoint.  No
  * reference counterpart (the reference's launch shapes are fixed,
  * generate_simulator.py:85-106). */
 int sss_plan_set_batch_config(sss_plan* plan, int lanes, int cta_threads,
