@@ -818,7 +818,11 @@ static int adjoint_slots_prepare(sss_plan* p, const BatchLayout& Ly, int ntraj, 
     BatchLayout& BL = *BLo;
     int rc = SSS_EINVAL;
     if (wide) {
-        rc = slots_layout_rows(p, brows, 64, 64, 8, Ly.active, brr, &BL);
+        rc = phased_layout_rows(p, brows, 64, 64, 8, Ly.active, brr, varies, &BL);
+        if (rc != SSS_OK) {
+            set_error("");
+            rc = slots_layout_rows(p, brows, 64, 64, 8, Ly.active, brr, &BL);
+        }
         if (rc != SSS_OK) set_error("");
     }
     if (rc != SSS_OK) {

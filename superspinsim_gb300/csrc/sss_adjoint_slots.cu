@@ -295,6 +295,28 @@ int launch_adj(sss_plan* p, Kern kern, const AdjSlotArgs& a, int threads, int sl
 int launch_adjoint_slots(sss_plan* p, int L, bool phased, int shape, int S, const AdjSlotArgs& a,
                          int threads, size_t smem, cudaStream_t st) {
     const int spc = threads / L;
+    static_assert(kPhasedShapeCount == 8, "one case per phased shape");
+#define SSS_ADJ_PHASED(LL, k)                                                                 \
+    case k:                                                                                   \
+        return launch_adj(p,                                                                  \
+                          k_adjoint_slots<LL, PhasedProgram<kPhasedShapes[k].C1,              \
+                                                            kPhasedShapes[k].P1,              \
+                                                            kPhasedShapes[k].C2,              \
+                                                            kPhasedShapes[k].P2>>,            \
+                          a, threads, spc, smem, st);
+    if (L == 64 && phased) {
+        switch (shape) {
+            SSS_ADJ_PHASED(64, 0)
+            SSS_ADJ_PHASED(64, 1)
+            SSS_ADJ_PHASED(64, 2)
+            SSS_ADJ_PHASED(64, 3)
+            SSS_ADJ_PHASED(64, 4)
+            SSS_ADJ_PHASED(64, 5)
+            SSS_ADJ_PHASED(64, 6)
+            SSS_ADJ_PHASED(64, 7)
+            default: return fail(SSS_EINVAL, "no phased adjoint kernel for this shape");
+        }
+    }
     if (L == 64 && !phased) {
         // one trajectory per 64-thread CTA: for batches too small to give
         // every SM sub-partition a warp at 32 lanes
@@ -309,28 +331,19 @@ int launch_adjoint_slots(sss_plan* p, int L, bool phased, int shape, int S, cons
     }
     if (L != 32) return fail(SSS_EINVAL, "the slot adjoint runs 32- or 64-lane groups");
     if (phased) {
-        static_assert(kPhasedShapeCount == 8, "one case per phased shape");
-#define SSS_ADJ_PHASED(k)                                                                     \
-    case k:                                                                                   \
-        return launch_adj(p,                                                                  \
-                          k_adjoint_slots<32, PhasedProgram<kPhasedShapes[k].C1,              \
-                                                            kPhasedShapes[k].P1,              \
-                                                            kPhasedShapes[k].C2,              \
-                                                            kPhasedShapes[k].P2>>,            \
-                          a, threads, spc, smem, st);
         switch (shape) {
-            SSS_ADJ_PHASED(0)
-            SSS_ADJ_PHASED(1)
-            SSS_ADJ_PHASED(2)
-            SSS_ADJ_PHASED(3)
-            SSS_ADJ_PHASED(4)
-            SSS_ADJ_PHASED(5)
-            SSS_ADJ_PHASED(6)
-            SSS_ADJ_PHASED(7)
+            SSS_ADJ_PHASED(32, 0)
+            SSS_ADJ_PHASED(32, 1)
+            SSS_ADJ_PHASED(32, 2)
+            SSS_ADJ_PHASED(32, 3)
+            SSS_ADJ_PHASED(32, 4)
+            SSS_ADJ_PHASED(32, 5)
+            SSS_ADJ_PHASED(32, 6)
+            SSS_ADJ_PHASED(32, 7)
             default: return fail(SSS_EINVAL, "no phased adjoint kernel for this shape");
         }
-#undef SSS_ADJ_PHASED
     }
+#undef SSS_ADJ_PHASED
     switch (S) {
         case 8: return launch_adj(p, k_adjoint_slots<32, SlotProgram<8>>, a, threads, spc, smem, st);
         case 10: return launch_adj(p, k_adjoint_slots<32, SlotProgram<10>>, a, threads, spc, smem, st);

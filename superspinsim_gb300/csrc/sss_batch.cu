@@ -1753,8 +1753,11 @@ int phased_layout_rows(sss_plan* p, const std::vector<std::vector<BatchLayout::E
                        BatchLayout* out) {
     BatchLayout& Ly = *out;
     const int M = (int)rows.size();
-    if (L != 8 && L != 16 && L != 32)
-        return fail(SSS_EINVAL, "phased row-part variant needs 8, 16 or 32 lanes per trajectory");
+    // the forward kernels compile phased programs for warp groups (8-32
+    // lanes); the adjoint's block series also for 64-lane groups
+    if (L != 8 && L != 16 && L != 32 && L != 64)
+        return fail(SSS_EINVAL, "phased row-part variant needs 8, 16, 32 or 64 lanes per trajectory");
+    if (L > 32) threads = L;  // a group wider than a warp is one CTA
     if (threads % L) return fail(SSS_EINVAL, "CTA size must be a multiple of the lanes per trajectory");
     if (M + 2 > (int)kSlotIdx) return fail(SSS_EINVAL, "phased row-part variant supports at most 16381 rows");
     std::vector<int> nent(M);
