@@ -46,6 +46,7 @@
 #include <cmath>
 #include <vector>
 
+#include "sss_adjoint_ring.cuh"
 #include "sss_adjoint_slots.cuh"
 #include "sss_device.cuh"
 #include "sss_internal.cuh"
@@ -92,13 +93,6 @@ __device__ __forceinline__ int wend(unsigned w) { return (int)(w >> 16); }
 // transposed-entry index flag: the differentiated generator is non-zero here
 constexpr int kHasG = 1 << 30;
 
-// segment of a channel's program (prog points at the channel) at time t,
-// or -1 past its last segment
-__device__ __forceinline__ int x_segment(const double* prog, int nseg, double t) {
-    for (int s = 0; s < nseg; s++)
-        if (t < prog[s * 5]) return s;
-    return -1;
-}
 
 template <int L>
 struct Group {
@@ -245,7 +239,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjArgs a) {
                                             __dmul_rn(a.dt, (double)t)),
                                   __ldg(a.noff + k));
             const double* dprog = prog + (size_t)a.dch * a.nseg * 5;
-            int s = x_segment(dprog, a.nseg, tn);
+            int s = channel_segment(dprog, a.nseg, tn);
             double cs = 0.0, dph = 0.0;
             if (s >= 0) {
                 const double* p = dprog + s * 5;
@@ -590,49 +584,9 @@ __global__ void __launch_bounds__(256, 1) k_adjoint_parts(const AdjPartsArgs a) 
                 // steps n, n-1, ..., n-kRing+1: node values of the live channels;
                 // for the differentiated channel also cos, -a sin, the segment
                 // and -a sin tau t
-                for (int i = li; i < kRing * Q * NL; i += L) {
-                    const int s = i / (Q * NL), rem = i - s * Q * NL, k = rem / NL, gi = rem - k * NL;
-                    const long ns = n - s;
-                    double val = 0.0, cs = 0.0, dph = 0.0, dfr = 0.0;
-                    int sg = -1;
-                    if (ns >= 0) {
-                        const int ts = (int)(ns / a.F), rs = (int)(ns % a.F);
-                        const double tn = __dadd_rn(__dadd_rn(__dadd_rn(a.t0, __ldg(a.toff + rs)),
-                                                              __dmul_rn(a.dt, (double)ts)),
-                                                    __ldg(a.noff + k));
-                        const int g = a.gen_index[a.live[gi]];
-                        if (gi == a.x_live) {
-                            sg = x_segment(dprog, a.nseg, tn);
-                            if (sg >= 0) {
-                                const double* q = dprog + sg * 5;
-                                const double arg =
-                                    __dadd_rn(__dmul_rn(__dmul_rn(6.283185307179586, q[3]), tn), q[4]);
-                                cs = cos(arg);
-                                dph = -q[2] * sin(arg);
-                                dfr = dph * (6.283185307179586 * tn);
-                                val = q[2] == 0.0 ? q[1] : __dadd_rn(q[1], __dmul_rn(q[2], cs));
-                            }
-                        } else {
-                            val = (g - 1 < a.nch) ? channel_value(prog, a.nseg, g - 1, tn) : 0.0;
-                        }
-                    }
-                    ringc[i] = val;
-                    if (gi == a.x_live) {
-                        double* rd = ring_d + (s * Q + k) * 4;
-                        rd[0] = cs;
-                        rd[1] = dph;
-                        rd[2] = (double)sg;
-                        rd[3] = dfr;
-                    }
-                }
+                adjoint_ring_nodes(a, prog, dprog, n, li, L, ringc, ring_d);
                 gsync();
-                for (int i = li; i < kRing * K * NL; i += L) {
-                    const int s = i / (K * NL), rem = i - s * K * NL, e = rem / NL, gi = rem - e * NL;
-                    double w = 0.0;
-                    for (int k = 0; k < Q; k++)
-                        w = fma(__ldg(a.W + e * Q + k), ringc[(s * Q + k) * NL + gi], w);
-                    ring_ag[i] = w * a.h;
-                }
+                adjoint_ring_weights(a, li, L, ringc, ring_ag);
                 gsync();
                 rp = 0;
             }
