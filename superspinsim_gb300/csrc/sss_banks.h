@@ -179,10 +179,14 @@ inline int optimise_banks(BankProblem& pb, std::vector<int>& pos, std::vector<in
         }
         return -1;
     };
-    // the temperature falls geometrically from 0.3 to 0.05 extra wavefronts
-    long spent = 0;
+    // the temperature falls geometrically from 0.3 to 0.05 extra wavefronts;
+    // the search stops early once a third of the budget passes without a
+    // new best
+    long spent = 0, spent_at_best = 0;
     const long max_iters = budget / 4 + 1;
-    for (long it = 0; spent < budget && it < max_iters && best_cost > 0; it++) {
+    for (long it = 0; spent < budget && it < max_iters && best_cost > 0 &&
+                      spent - spent_at_best <= budget / 3;
+         it++) {
         const double temp = 0.3 * std::pow(0.05 / 0.3, (double)spent / (double)budget);
         const double u = uni(rng) * (double)n_moves;
         int kind = u < (double)n_labels ? 0 : 1;
@@ -259,6 +263,7 @@ inline int optimise_banks(BankProblem& pb, std::vector<int>& pos, std::vector<in
                 best_pos = pos;
                 best_cell = pb.cell;
                 best_origin = origin;
+                spent_at_best = spent;
             }
         } else {
             apply();  // every move is its own inverse

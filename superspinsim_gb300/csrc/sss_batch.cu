@@ -1646,8 +1646,9 @@ static int bank_relabel(sss_plan* p, BatchLayout& Ly, const std::vector<int>& ac
         pb.cell = moved;
         after = bank_total_cost(pb, pos);
     } else {
-        // about 0.1 s of host time for NV-7 (26 labels), 1 s for NV-21 (249)
-        const long budget = std::min<long>(6000000L, 300000L + 20000L * (long)(M + np));
+        // at most a few seconds of host time, once per layout (NV-21's
+        // 249 labels: about 2.5 s; NV-7 converges in a fraction of that)
+        const long budget = std::min<long>(20000000L, 300000L + 80000L * (long)(M + np));
         after = optimise_banks(pb, pos, origin, budget, &before);
         origin.resize(n_load);
         std::vector<int> entry(pos);
