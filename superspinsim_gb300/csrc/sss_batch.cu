@@ -1896,20 +1896,24 @@ static double layout_cost(const BatchLayout& Ly) {
 // Automatic lane count for n trajectories, from the cost of the best layout
 // at each lane count 8, 16, ..., 256 (0: does not fit): the count whose
 // busiest SM sub-partition issues the fewest FP64 instructions per Horner
-// term, ceil(warps / sub-partitions) * cost; ties go to the wider group (more
-// warps to hide latency).  0 when nothing fits.
+// term, ceil(warps / sub-partitions) * cost.  On a tie the narrower group
+// wins once its warps fill every sub-partition (the same FP64 issue count
+// with fewer group barriers and shuffles per instruction); before that the
+// wider one does (more warps to hide latency).  0 when nothing fits.
 int auto_lanes(const sss_plan* p, const double* cost, long n) {
     int best = 0;
     double best_v = 0.0;
+    long best_warps = 0;
     const long subparts = 4L * p->num_sms;
     for (int i = 0; i < kLaneCounts; i++) {
         if (cost[i] <= 0.0) continue;
         const long Lc = 8L << i;
         const long warps = (std::max(1L, n) * Lc + 31) / 32;
         const double v = (double)((warps + subparts - 1) / subparts) * cost[i];
-        if (!best || v <= best_v) {
+        if (!best || v < best_v || (v == best_v && best_warps < subparts)) {
             best = (int)Lc;
             best_v = v;
+            best_warps = warps;
         }
     }
     return best;
@@ -2638,11 +2642,13 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
         }
         if (!phased || !Ly.parts) break;
         // the next phase starts at the first sample where the automatic
-        // lane count for the trajectories still running changes
+        // lane count for the trajectories still running exceeds this one
+        // (phases only widen; where the count drops back to a narrower group
+        // on a tie the phase runs on)
         const int n_now = running_after(p, t);
         int n_next = -1;
         for (int n = n_now - 1; n >= 1; n--)
-            if (auto_lanes(p, p->auto_cost, n) != Ly.L) {
+            if (auto_lanes(p, p->auto_cost, n) > Ly.L) {
                 n_next = n;
                 break;
             }

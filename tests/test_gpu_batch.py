@@ -375,7 +375,7 @@ def test_dropin_simulate_nv21_uses_batched_trace():
 
 def test_phased_uneven_batch_chunked_graph_and_oracle():
     """3000 short uneven Ramsey trajectories: enough for the automatic lanes
-    to widen in phases (8 lanes while 2432 or more run, then 16, then 32).
+    to widen in phases as trajectories finish (16 lanes, then 32 and wider).
     The one-shot run, a chunked run and its CUDA-graph capture -- all
     prepared with the sample counts -- agree bit for bit (the same layout
     at every output sample), and sampled trajectories match the oracle."""
