@@ -1893,30 +1893,11 @@ static double layout_cost(const BatchLayout& Ly) {
     return c;
 }
 
-// Automatic lane count for n trajectories, from the cost of the best layout
-// at each lane count 8, 16, ..., 256 (0: does not fit): the count whose
-// busiest SM sub-partition issues the fewest FP64 instructions per Horner
-// term, ceil(warps / sub-partitions) * cost.  On a tie the narrower group
-// wins once its warps fill every sub-partition (the same FP64 issue count
-// with fewer group barriers and shuffles per instruction); before that the
-// wider one does (more warps to hide latency).  0 when nothing fits.
+// Automatic lane count for n trajectories (auto_lane_count on this GPU's
+// sub-partitions) from the cost of the best layout at each lane count 8,
+// 16, ..., 256 (0: does not fit).  0 when nothing fits.
 int auto_lanes(const sss_plan* p, const double* cost, long n) {
-    int best = 0;
-    double best_v = 0.0;
-    long best_warps = 0;
-    const long subparts = 4L * p->num_sms;
-    for (int i = 0; i < kLaneCounts; i++) {
-        if (cost[i] <= 0.0) continue;
-        const long Lc = 8L << i;
-        const long warps = (std::max(1L, n) * Lc + 31) / 32;
-        const double v = (double)((warps + subparts - 1) / subparts) * cost[i];
-        if (!best || v < best_v || (v == best_v && best_warps < subparts)) {
-            best = (int)Lc;
-            best_v = v;
-            best_warps = warps;
-        }
-    }
-    return best;
+    return auto_lane_count(4L * p->num_sms, cost, n);
 }
 
 int build_layout(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
@@ -2518,10 +2499,7 @@ static int make_args(sss_plan* p, const BatchLayout& Ly, int ntraj, int nch, int
 }
 
 // trajectories of a prepared batch with more than t output samples
-static int running_after(const sss_plan* p, int t) {
-    const std::vector<int>& lo = p->batch_longest;
-    return (int)(std::lower_bound(lo.begin(), lo.end(), t, std::greater<int>()) - lo.begin());
-}
+static int running_after(const sss_plan* p, int t) { return running_after(p->batch_longest, t); }
 
 int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nseg,
                   const double* d_prog, double dt, int F, const double* h_rw, cudaStream_t st,
@@ -2645,13 +2623,7 @@ int batch_prepare(sss_plan* p, int ntraj, const double* d_rho0, int nch, int nse
         // lane count for the trajectories still running exceeds this one
         // (phases only widen; where the count drops back to a narrower group
         // on a tie the phase runs on)
-        const int n_now = running_after(p, t);
-        int n_next = -1;
-        for (int n = n_now - 1; n >= 1; n--)
-            if (auto_lanes(p, p->auto_cost, n) > Ly.L) {
-                n_next = n;
-                break;
-            }
+        const int n_next = phase_end_count(4L * p->num_sms, p->auto_cost, Ly.L, running_after(p, t));
         if (n_next < 0 || p->batch_longest[n_next] <= t) break;
         t = p->batch_longest[n_next];
     }

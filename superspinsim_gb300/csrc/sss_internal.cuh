@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "sss.h"
+#include "sss_lanes.h"
 
 namespace sss {
 
@@ -25,7 +26,6 @@ constexpr int kRing = 16;       // fine steps of coefficients per refill
 constexpr int kPartShapes[][2] = {{1, 4}, {2, 4}, {4, 4}, {2, 8}};
 // slot-packed kernels: slots per lane (S <= kSlotsMax)
 constexpr int kSlotsMax = 16;
-constexpr int kLaneCounts = 6;  // lanes per trajectory 8, 16, ..., 256 of the row kernels
 
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
